@@ -1,0 +1,972 @@
+// Plan, run loop, diagnostics / initial-condition kernels and the C ABI
+// (include/tgdns.h) of the GB300-native Taylor-Green time step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/tgdns.h"
+#include "tg_common.cuh"
+
+namespace tg {
+
+// pass-kernel launchers, one per instantiated (real type, size): tg_inst.cu
+#define TG_SIZES_F32(X) X(float, 8) X(float, 12) X(float, 16) X(float, 24) X(float, 32) X(float, 48) \
+  X(float, 64) X(float, 96) X(float, 128) X(float, 256) X(float, 512)
+#define TG_SIZES_F64(X) X(double, 8) X(double, 16) X(double, 32) X(double, 64) X(double, 96) \
+  X(double, 128) X(double, 256)
+#define TG_DECL(R, N) cudaError_t launch_##R##_##N(int, const PassArgs<R>&, int, cudaStream_t);
+TG_SIZES_F32(TG_DECL)
+TG_SIZES_F64(TG_DECL)
+#undef TG_DECL
+
+enum PassOpHost {
+  OP_KX_STAGE3 = 0, OP_KX_STAGE6, OP_KX_LOAD3, OP_KX_LOAD6, OP_KX_FWD3, OP_KX_FWD6,
+  OP_KY_INV, OP_KY_FWD, OP_KZ_PROD_HD, OP_KZ_PROD_MHD, OP_KZ_C2R, OP_KZ_R2C
+};
+
+template <typename R> using LaunchFn = cudaError_t (*)(int, const PassArgs<R>&, int, cudaStream_t);
+
+static LaunchFn<float> find_f32(int n) {
+  switch (n) {
+#define TG_CASE(R, N) case N: return &launch_##R##_##N;
+    TG_SIZES_F32(TG_CASE)
+#undef TG_CASE
+    default: return nullptr;
+  }
+}
+static LaunchFn<double> find_f64(int n) {
+  switch (n) {
+#define TG_CASE(R, N) case N: return &launch_##R##_##N;
+    TG_SIZES_F64(TG_CASE)
+#undef TG_CASE
+    default: return nullptr;
+  }
+}
+
+// ------------------------------------------------------------------ generic kernels
+constexpr int kDiagBlocks = 96;
+constexpr int kDiagThreads = 256;
+constexpr int kNQ = 5;  // E_k, enstrophy, sum w k^2 |u|^2, E_m, H_c
+
+struct Neumaier {
+  double s = 0.0, c = 0.0;
+  __device__ __forceinline__ void add(double x) {
+    const double t = s + x;
+    c += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return s + c; }
+};
+
+template <typename R>
+__global__ void __launch_bounds__(kDiagThreads) diag_partial(const cplx<R>* S, Geo g, int F, double* part) {
+  using C = cplx<R>;
+  const int run = blockIdx.y;
+  const C* base = S + (long long)run * F * g.sS;
+  const long long total = (long long)g.M * g.M * g.Hk;
+  Neumaier q[kNQ];
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int kz = int(idx % g.Hk);
+    const long long r = idx / g.Hk;
+    const int iyc = int(r % g.M), ic = int(r / g.M);
+    const double kx = ksigned(ic, g.K), ky = ksigned(iyc, g.K), kzd = kz;
+    const double w = (kz == 0) ? 1.0 : 2.0;
+    const long long o = ((long long)ic * g.M + iyc) * g.Hz + kz;
+    const C ux = base[o], uy = base[g.sS + o], uz = base[2 * g.sS + o];
+    const double e2 = double(ux.x) * ux.x + double(ux.y) * ux.y + double(uy.x) * uy.x +
+                      double(uy.y) * uy.y + double(uz.x) * uz.x + double(uz.y) * uz.y;
+    // |k x u|^2 with complex components
+    const double cxr = ky * uz.x - kzd * uy.x, cxi = ky * uz.y - kzd * uy.y;
+    const double cyr = kzd * ux.x - kx * uz.x, cyi = kzd * ux.y - kx * uz.y;
+    const double czr = kx * uy.x - ky * ux.x, czi = kx * uy.y - ky * ux.y;
+    const double c2 = cxr * cxr + cxi * cxi + cyr * cyr + cyi * cyi + czr * czr + czi * czi;
+    q[0].add(0.5 * w * e2);
+    q[1].add(0.5 * w * c2);
+    q[2].add(w * (kx * kx + ky * ky + kzd * kzd) * e2);
+    if (F == 6) {
+      const C bx = base[3 * g.sS + o], by = base[4 * g.sS + o], bz = base[5 * g.sS + o];
+      const double b2 = double(bx.x) * bx.x + double(bx.y) * bx.y + double(by.x) * by.x +
+                        double(by.y) * by.y + double(bz.x) * bz.x + double(bz.y) * bz.y;
+      const double hc = double(ux.x) * bx.x + double(ux.y) * bx.y + double(uy.x) * by.x +
+                        double(uy.y) * by.y + double(uz.x) * bz.x + double(uz.y) * bz.y;
+      q[3].add(0.5 * w * b2);
+      q[4].add(w * hc);
+    }
+  }
+  __shared__ double sh[kNQ][kDiagThreads];
+  for (int i = 0; i < kNQ; ++i) sh[i][threadIdx.x] = q[i].value();
+  __syncthreads();
+  for (int s = kDiagThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int i = 0; i < kNQ; ++i) sh[i][threadIdx.x] += sh[i][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x < kNQ) part[((long long)run * gridDim.x + blockIdx.x) * kNQ + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// one block per run: fixed-order compensated sum of the partials, one record
+__global__ void diag_final(const double* part, int nblk, const RunCoef* coef, const unsigned long long* amax,
+                           int namax, int F, double* out) {
+  const int run = blockIdx.x;
+  __shared__ double v[kNQ];
+  if (threadIdx.x < kNQ) {
+    Neumaier s;
+    for (int b = 0; b < nblk; ++b) s.add(part[((long long)run * nblk + b) * kNQ + threadIdx.x]);
+    v[threadIdx.x] = s.value();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double* o = out + (long long)run * TG_DIAG_WIDTH;
+    o[TG_D_KINETIC] = v[0];
+    o[TG_D_ENSTROPHY] = v[1];
+    o[TG_D_DISSIPATION] = coef[run].nu * v[2];
+    o[TG_D_MAGNETIC] = (F == 6) ? v[3] : 0.0;
+    o[TG_D_CROSS_HELICITY] = (F == 6) ? v[4] : 0.0;
+    o[TG_D_TOTAL] = v[0] + ((F == 6) ? v[3] : 0.0);
+    o[TG_D_DIVU_MAX] = (namax > 0) ? __longlong_as_double((long long)amax[run * namax]) : 0.0;
+    o[TG_D_DIVB_MAX] = (namax > 1) ? __longlong_as_double((long long)amax[run * namax + 1]) : 0.0;
+  }
+}
+
+__global__ void amax_to_double(const unsigned long long* amax, int count, double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) out[i] = __longlong_as_double((long long)amax[i]);
+}
+
+// analytic Fourier coefficients of the Taylor-Green fields (modes |k_i| = 1)
+template <typename R>
+__global__ void ic_kernel(cplx<R>* S, Geo g, int F, int batch, int kind, double b_amp) {
+  using C = cplx<R>;
+  const long long per_run = (long long)F * g.sS;
+  const long long total = per_run * batch;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long r = idx % per_run;
+    const int f = int(r / g.sS);
+    const long long m = r % g.sS;
+    const int kz = int(m % g.Hz);
+    const int iyc = int((m / g.Hz) % g.M), ic = int(m / ((long long)g.Hz * g.M));
+    const int kx = ksigned(ic, g.K), ky = ksigned(iyc, g.K);
+    double re = 0.0, im = 0.0;
+    if (kz == 1 && (kx == 1 || kx == -1) && (ky == 1 || ky == -1) && kind != TG_IC_ZERO) {
+      const double sx = kx, sy = ky, sz = 1.0;
+      const int c = f % 3;
+      if (f < 3) {  // u = (sin x cos y cos z, -cos x sin y cos z, 0)
+        if (c == 0) im = -sx / 8.0;
+        if (c == 1) im = sy / 8.0;
+      } else if (kind == TG_IC_MHD_REFERENCE) {
+        if (c == 0) im = -b_amp * sx / 8.0;
+        if (c == 1) im = b_amp * sy / 8.0;
+      } else if (kind == TG_IC_MHD_EQUAL_ENERGY) {
+        const double s = 1.0 / sqrt(3.0);
+        if (c == 0) re = -s * sy * sz / 8.0;
+        if (c == 1) re = -s * sx * sz / 8.0;
+        if (c == 2) re = s * sx * sy / 4.0;
+      }
+    }
+    C v;
+    v.x = R(re);
+    v.y = R(im);
+    S[idx] = v;
+  }
+}
+
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
+  unsigned long long z = x + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ double uniform53(unsigned long long h) {
+  return (double(h >> 11) + 1.0) * (1.0 / 9007199254740992.0);
+}
+
+// Seeded divergence-free perturbation (unnormalised) of the velocity, written to
+// P[run][3][M][M][Hz]; the definition is the one documented in include/tgdns.h.
+template <typename R>
+__global__ void pert_kernel(cplx<R>* P, Geo g, int batch, unsigned long long seed, double k0) {
+  using C = cplx<R>;
+  const long long per_run = (long long)g.M * g.M * g.Hk;
+  const long long total = per_run * batch;
+  const int N = g.n, H = g.n / 2 + 1;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int run = int(idx / per_run);
+    const long long m = idx % per_run;
+    const int kz = int(m % g.Hk);
+    const int iyc = int((m / g.Hk) % g.M), ic = int(m / ((long long)g.Hk * g.M));
+    int kx = ksigned(ic, g.K), ky = ksigned(iyc, g.K);
+    // kz = 0 plane: the lower half takes the conjugate of its mirror mode
+    const bool lower = (kz == 0) && (ky < 0 || (ky == 0 && kx < 0));
+    const int gx = lower ? -kx : kx, gy = lower ? -ky : ky;
+    const unsigned long long key = splitmix64(seed + (unsigned long long)run);
+    const unsigned long long ix = (unsigned long long)((gx + N) % N), iy = (unsigned long long)((gy + N) % N);
+    double gr[3], gi[3];
+    for (int c = 0; c < 3; ++c) {
+      const unsigned long long cnt = ((((unsigned long long)c * N + ix) * N + iy) * H + kz) * 2ull;
+      const double u1 = uniform53(splitmix64(key ^ cnt));
+      const double u2 = uniform53(splitmix64(key ^ (cnt + 1ull)));
+      const double rr = sqrt(-2.0 * log(u1));
+      const double th = 2.0 * 3.141592653589793 * u2;
+      gr[c] = rr * cos(th);
+      gi[c] = rr * sin(th);
+    }
+    const double fx = gx, fy = gy, fz = kz;
+    const double k2 = fx * fx + fy * fy + fz * fz;
+    const double k2s = (k2 == 0.0) ? 1.0 : k2;
+    const double kdr = fx * gr[0] + fy * gr[1] + fz * gr[2];
+    const double kdi = fx * gi[0] + fy * gi[1] + fz * gi[2];
+    const double kk[3] = {fx, fy, fz};
+    const double amp = (k2 == 0.0) ? 0.0 : sqrt(k2) * exp(-k2 / (k0 * k0));
+    const long long base = (long long)run * 3 * g.sS + ((long long)ic * g.M + iyc) * g.Hz + kz;
+    for (int c = 0; c < 3; ++c) {
+      double vr = (gr[c] - kk[c] * kdr / k2s) * amp;
+      double vi = (gi[c] - kk[c] * kdi / k2s) * amp;
+      if (lower) vi = -vi;
+      C v;
+      v.x = R(vr);
+      v.y = R(vi);
+      P[base + c * g.sS] = v;
+    }
+  }
+}
+
+template <typename R>
+__global__ void axpy_pert(cplx<R>* S, const cplx<R>* P, Geo g, int F, int batch, const double* scale) {
+  const long long per = 3 * g.sS;
+  const long long total = per * batch;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int run = int(idx / per);
+    const long long o = (long long)run * F * g.sS + idx % per;
+    const double s = scale[run];
+    cplx<R> v = S[o];
+    const cplx<R> p = P[idx];
+    v.x = R(double(v.x) + s * double(p.x));
+    v.y = R(double(v.y) + s * double(p.y));
+    S[o] = v;
+  }
+}
+
+
+// compact state -> full fftn layout (x N^3, Hermitian completion for kz > N/2)
+template <typename R>
+__global__ void to_full_kernel(const cplx<R>* S, cplx<R>* out, Geo g, int F, int batch) {
+  using C = cplx<R>;
+  const int N = g.n;
+  const long long n3 = (long long)N * N * N;
+  const long long total = n3 * F * batch;
+  const double scale = double(N) * N * N;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long rf = idx / n3;  // run * F + f
+    const long long m = idx % n3;
+    const int kzr = int(m % N), kyr = int((m / N) % N), kxr = int(m / ((long long)N * N));
+    double re = 0.0, im = 0.0;
+    int ic, iyc, kz;
+    bool conj = false, ok = false;
+    if (kzr <= g.K) {
+      ic = kcompact(kxr, N, g.K); iyc = kcompact(kyr, N, g.K); kz = kzr; ok = ic >= 0 && iyc >= 0;
+    } else if (kzr >= N - g.K) {
+      ic = kcompact((N - kxr) % N, N, g.K); iyc = kcompact((N - kyr) % N, N, g.K); kz = N - kzr;
+      ok = ic >= 0 && iyc >= 0; conj = true;
+    }
+    if (ok) {
+      const C v = S[rf * g.sS + ((long long)ic * g.M + iyc) * g.Hz + kz];
+      re = double(v.x) * scale;
+      im = (conj ? -double(v.y) : double(v.y)) * scale;
+    }
+    C o;
+    o.x = R(re);
+    o.y = R(im);
+    out[idx] = o;
+  }
+}
+
+// full fftn layout -> compact state (kept modes, / N^3); padding rows zeroed
+template <typename R>
+__global__ void from_full_kernel(const cplx<R>* full, cplx<R>* S, Geo g, int F, int batch) {
+  using C = cplx<R>;
+  const int N = g.n;
+  const long long n3 = (long long)N * N * N;
+  const long long total = g.sS * F * batch;
+  const double inv = 1.0 / (double(N) * N * N);
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long rf = idx / g.sS;
+    const long long m = idx % g.sS;
+    const int kz = int(m % g.Hz), iyc = int((m / g.Hz) % g.M), ic = int(m / ((long long)g.Hz * g.M));
+    C o;
+    o.x = R(0);
+    o.y = R(0);
+    if (kz <= g.K) {
+      const C v = full[rf * n3 + ((long long)kfull(ic, N, g.K) * N + kfull(iyc, N, g.K)) * N + kz];
+      o.x = R(double(v.x) * inv);
+      o.y = R(double(v.y) * inv);
+    }
+    S[idx] = o;
+  }
+}
+
+// 0.5 <sum_c u_c^2> of physical fields, groups of 3 components: partial sums
+template <typename R>
+__global__ void __launch_bounds__(kDiagThreads) phys_energy_partial(const R* u, long long n3, double* part) {
+  const int grp = blockIdx.y;  // (run * F + 3 * j) / 3
+  const R* base = u + (long long)grp * 3 * n3;
+  Neumaier q;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (long long)gridDim.x * blockDim.x) {
+    const double a = base[i], b = base[n3 + i], c = base[2 * n3 + i];
+    q.add(a * a + b * b + c * c);
+  }
+  __shared__ double sh[kDiagThreads];
+  sh[threadIdx.x] = q.value();
+  __syncthreads();
+  for (int s = kDiagThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[(long long)grp * gridDim.x + blockIdx.x] = sh[0];
+}
+
+__global__ void phys_energy_final(const double* part, int nblk, int groups, long long n3, double* out) {
+  const int grp = blockIdx.x * blockDim.x + threadIdx.x;
+  if (grp >= groups) return;
+  Neumaier s;
+  for (int b = 0; b < nblk; ++b) s.add(part[(long long)grp * nblk + b]);
+  out[grp] = 0.5 * s.value() / double(n3);
+}
+}  // namespace tg
+
+// ====================================================================== plan
+using namespace tg;
+
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+static int cuda_fail(cudaError_t e, const char* where) {
+  return fail(TG_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define TG_CUDA(call, where)                      \
+  do {                                            \
+    cudaError_t e_ = (call);                      \
+    if (e_ != cudaSuccess) return cuda_fail(e_, where); \
+  } while (0)
+
+struct tg_plan {
+  Geo g{};
+  int n = 0, K = 0, batch = 1, F = 3, G = 6, physics = 0, prec = 0, flags = 0;
+  cudaStream_t st = nullptr;
+  void* X = nullptr;    // [batch][G][N][M][Hz]
+  void* Y = nullptr;    // [batch][G][N][N][Hz]; W aliases it
+  void* Z = nullptr;    // [batch][F][N][N][Hz]
+  void* ACC = nullptr;  // [batch][F][M][M][Hz]
+  void* VS = nullptr;   // explicit-viscosity stage state
+  void* TW = nullptr;   // W_N^m
+  double* part = nullptr;
+  double* dtmp = nullptr;  // [batch][TG_DIAG_WIDTH] scratch record
+  unsigned long long* amax = nullptr;
+  RunCoef* coef = nullptr;
+  std::vector<RunCoef> hcoef;
+  LaunchFn<float> l32 = nullptr;
+  LaunchFn<double> l64 = nullptr;
+  cudaGraphExec_t step_exec = nullptr;
+  cudaGraph_t step_graph = nullptr;
+  const void* step_state = nullptr;
+  int64_t launches = 0;
+  int64_t scratch = 0;
+};
+
+namespace {
+
+size_t csize(const tg_plan* p) { return p->prec == TG_PREC_F64 ? 16 : 8; }
+
+template <typename R> LaunchFn<R> launcher(const tg_plan* p);
+template <> LaunchFn<float> launcher<float>(const tg_plan* p) { return p->l32; }
+template <> LaunchFn<double> launcher<double>(const tg_plan* p) { return p->l64; }
+
+template <typename R>
+struct Ops {
+  using C = cplx<R>;
+
+  static PassArgs<R> base(tg_plan* p) {
+    PassArgs<R> a;
+    std::memset(&a, 0, sizeof(a));
+    a.g = p->g;
+    a.tw = static_cast<const C*>(p->TW);
+    a.coef = p->coef;
+    a.amax = p->amax;
+    if (p->flags & TG_FLAG_EXPLICIT_VISC) a.flags |= FLAG_EXPLICIT;
+    return a;
+  }
+  static int go(tg_plan* p, int op, const PassArgs<R>& a, const char* what) {
+    cudaError_t e = launcher<R>(p)(op, a, p->batch, p->st);
+    ++p->launches;
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    return TG_OK;
+  }
+  // spectral state -> inverse-x of nout fields (map) into X
+  static int load_inv(tg_plan* p, const void* S, int map, int nin, int nout) {
+    PassArgs<R> a = base(p);
+    a.spec_in = static_cast<const C*>(S);
+    a.out = static_cast<C*>(p->X);
+    a.map = map;
+    a.nin = nin;
+    a.nout = nout;
+    return go(p, p->F == 6 ? OP_KX_LOAD6 : OP_KX_LOAD3, a, "kx load");
+  }
+  static int y_inv(tg_plan* p, int nf) {
+    PassArgs<R> a = base(p);
+    a.in = static_cast<const C*>(p->X);
+    a.out = static_cast<C*>(p->Y);
+    a.nin = a.nout = nf;
+    return go(p, OP_KY_INV, a, "ky inverse");
+  }
+  static int z_prod(tg_plan* p) {
+    PassArgs<R> a = base(p);
+    a.in = static_cast<const C*>(p->Y);
+    a.out = static_cast<C*>(p->Z);
+    a.nin = p->G;
+    a.nout = p->F;
+    return go(p, p->F == 6 ? OP_KZ_PROD_MHD : OP_KZ_PROD_HD, a, "kz product");
+  }
+  static int y_fwd(tg_plan* p, int nf) {
+    PassArgs<R> a = base(p);
+    a.in = static_cast<const C*>(p->Z);
+    a.out = static_cast<C*>(p->Y);  // W aliases Y
+    a.nin = a.nout = nf;
+    return go(p, OP_KY_FWD, a, "ky forward");
+  }
+  static int x_stage(tg_plan* p, void* S, int stage) {
+    PassArgs<R> a = base(p);
+    a.in = static_cast<const C*>(p->Y);
+    a.out = static_cast<C*>(p->X);
+    a.S = static_cast<C*>(S);
+    a.acc = static_cast<C*>(p->ACC);
+    a.vs = static_cast<C*>(p->VS);
+    a.stage = stage;
+    a.nin = p->F;
+    a.nout = p->G;
+    return go(p, p->F == 6 ? OP_KX_STAGE6 : OP_KX_STAGE3, a, "kx stage");
+  }
+  static int x_fwd(tg_plan* p, void* out, const void* spec_in, bool rhs) {
+    PassArgs<R> a = base(p);
+    a.in = static_cast<const C*>(p->Y);
+    a.spec_out = static_cast<C*>(out);
+    a.spec_in = static_cast<const C*>(spec_in);
+    a.nin = p->F;
+    if (rhs) a.flags |= FLAG_RHS;
+    return go(p, p->F == 6 ? OP_KX_FWD6 : OP_KX_FWD3, a, "kx forward");
+  }
+  static int z_c2r(tg_plan* p, void* phys, int nf, bool amax) {
+    PassArgs<R> a = base(p);
+    a.in = static_cast<const C*>(p->Y);
+    a.phys_out = static_cast<R*>(phys);
+    a.nin = nf;
+    if (amax) a.flags |= FLAG_AMAX;
+    return go(p, OP_KZ_C2R, a, "kz c2r");
+  }
+  static int z_r2c(tg_plan* p, const void* phys, int nf) {
+    PassArgs<R> a = base(p);
+    a.phys_in = static_cast<const R*>(phys);
+    a.out = static_cast<C*>(p->Z);
+    a.nin = nf;
+    return go(p, OP_KZ_R2C, a, "kz r2c");
+  }
+  static int stages(tg_plan* p, void* S) {
+    for (int s = 1; s <= 4; ++s) {
+      int rc;
+      if ((rc = y_inv(p, p->G))) return rc;
+      if ((rc = z_prod(p))) return rc;
+      if ((rc = y_fwd(p, p->F))) return rc;
+      if ((rc = x_stage(p, S, s))) return rc;
+    }
+    return TG_OK;
+  }
+  static int start(tg_plan* p, const void* S) {
+    return load_inv(p, S, p->F == 6 ? MAP_UWBJ : MAP_UW, p->F, p->G);
+  }
+  static int diagnostics(tg_plan* p, const void* S, double* out) {
+    int rc;
+    const int nd = p->F / 3;
+    TG_CUDA(cudaMemsetAsync(p->amax, 0, sizeof(unsigned long long) * p->batch * 2, p->st), "memset");
+    if ((rc = load_inv(p, S, MAP_DIV, p->F, nd))) return rc;
+    if ((rc = y_inv(p, nd))) return rc;
+    {
+      PassArgs<R> a = base(p);
+      a.in = static_cast<const C*>(p->Y);
+      a.phys_out = nullptr;
+      a.nin = nd;
+      a.amax = p->amax;
+      a.flags |= FLAG_AMAX;
+      if ((rc = go(p, OP_KZ_C2R, a, "kz divergence"))) return rc;
+    }
+    dim3 grid(kDiagBlocks, p->batch);
+    diag_partial<R><<<grid, kDiagThreads, 0, p->st>>>(static_cast<const C*>(S), p->g, p->F, p->part);
+    TG_CUDA(cudaGetLastError(), "diag_partial");
+    diag_final<<<p->batch, 32, 0, p->st>>>(p->part, kDiagBlocks, p->coef, p->amax, nd, p->F, out);
+    TG_CUDA(cudaGetLastError(), "diag_final");
+    p->launches += 2;
+    return TG_OK;
+  }
+  static int absmax(tg_plan* p, const void* S, int which, double* out) {
+    int rc;
+    const int nf = (which == TG_ABSMAX_DIVERGENCE) ? p->F / 3 : p->F;
+    TG_CUDA(cudaMemsetAsync(p->amax, 0, sizeof(unsigned long long) * p->batch * nf, p->st), "memset");
+    if ((rc = load_inv(p, S, which == TG_ABSMAX_DIVERGENCE ? MAP_DIV : MAP_ID, p->F, nf))) return rc;
+    if ((rc = y_inv(p, nf))) return rc;
+    PassArgs<R> a = base(p);
+    a.in = static_cast<const C*>(p->Y);
+    a.nin = nf;
+    a.flags |= FLAG_AMAX;
+    if ((rc = go(p, OP_KZ_C2R, a, "kz absmax"))) return rc;
+    const int cnt = p->batch * nf;
+    amax_to_double<<<(cnt + 127) / 128, 128, 0, p->st>>>(p->amax, cnt, out);
+    TG_CUDA(cudaGetLastError(), "amax_to_double");
+    return TG_OK;
+  }
+
+  static int derived(tg_plan* p, const void* S, int which, void* phys) {
+    int rc;
+    const int nf = (which == TG_DERIVED_DIVERGENCE) ? p->F / 3 : p->F;
+    if ((rc = load_inv(p, S, which == TG_DERIVED_DIVERGENCE ? MAP_DIV : MAP_CURL, p->F, nf))) return rc;
+    if ((rc = y_inv(p, nf))) return rc;
+    return z_c2r(p, phys, nf, false);
+  }
+  static int full(tg_plan* p, const void* S, void* out, bool to_full) {
+    const long long total = to_full ? (long long)p->g.sP * p->F * p->batch : p->g.sS * p->F * p->batch;
+    const int blocks = (int)std::min<long long>((total + 255) / 256, 8192);
+    if (to_full)
+      to_full_kernel<R><<<blocks, 256, 0, p->st>>>(static_cast<const C*>(S), static_cast<C*>(out), p->g, p->F, p->batch);
+    else
+      from_full_kernel<R><<<blocks, 256, 0, p->st>>>(static_cast<const C*>(S), static_cast<C*>(out), p->g, p->F, p->batch);
+    TG_CUDA(cudaGetLastError(), "full spectrum conversion");
+    ++p->launches;
+    return TG_OK;
+  }
+  static int energy(tg_plan* p, const void* phys, double* out) {
+    const int groups = p->batch * (p->F / 3);
+    dim3 grid(kDiagBlocks, groups);
+    // the partial buffer holds batch * kDiagBlocks * kNQ doubles >= groups * kDiagBlocks
+    phys_energy_partial<R><<<grid, kDiagThreads, 0, p->st>>>(static_cast<const R*>(phys), p->g.sP, p->part);
+    TG_CUDA(cudaGetLastError(), "phys_energy_partial");
+    phys_energy_final<<<(groups + 63) / 64, 64, 0, p->st>>>(p->part, kDiagBlocks, groups, p->g.sP, out);
+    TG_CUDA(cudaGetLastError(), "phys_energy_final");
+    p->launches += 2;
+    return TG_OK;
+  }
+  static int initial(tg_plan* p, int kind, uint64_t seed, double amp, double k0, double b_amp, void* S) {
+    const long long total = (long long)p->batch * p->F * p->g.sS;
+    ic_kernel<R><<<(int)std::min<long long>((total + 255) / 256, 4096), 256, 0, p->st>>>(
+        static_cast<C*>(S), p->g, p->F, p->batch, kind, b_amp);
+    TG_CUDA(cudaGetLastError(), "ic_kernel");
+    if (amp > 0.0) {
+      const long long modes = (long long)p->batch * p->g.M * p->g.M * p->g.Hk;
+      C* P = static_cast<C*>(p->ACC);  // scratch: [batch][3][M][M][Hz]
+      TG_CUDA(cudaMemsetAsync(P, 0, csize(p) * 3 * p->g.sS * p->batch, p->st), "memset");
+      pert_kernel<R><<<(int)std::min<long long>((modes + 255) / 256, 4096), 256, 0, p->st>>>(
+          P, p->g, p->batch, (unsigned long long)seed, k0);
+      TG_CUDA(cudaGetLastError(), "pert_kernel");
+      dim3 grid(kDiagBlocks, p->batch);
+      diag_partial<R><<<grid, kDiagThreads, 0, p->st>>>(P, p->g, 3, p->part);
+      diag_final<<<p->batch, 32, 0, p->st>>>(p->part, kDiagBlocks, p->coef, p->amax, 0, 3, p->dtmp);
+      TG_CUDA(cudaGetLastError(), "perturbation energy");
+      std::vector<double> rec((size_t)p->batch * TG_DIAG_WIDTH), scale(p->batch);
+      TG_CUDA(cudaMemcpyAsync(rec.data(), p->dtmp, rec.size() * sizeof(double), cudaMemcpyDeviceToHost, p->st),
+              "memcpy");
+      TG_CUDA(cudaStreamSynchronize(p->st), "sync");
+      for (int r = 0; r < p->batch; ++r) {
+        const double e = rec[(size_t)r * TG_DIAG_WIDTH + TG_D_KINETIC];  // 0.5 <|v|^2>
+        scale[r] = (e > 0.0) ? amp / std::sqrt(2.0 * e / 3.0) : 0.0;
+      }
+      TG_CUDA(cudaMemcpyAsync(p->dtmp, scale.data(), scale.size() * sizeof(double), cudaMemcpyHostToDevice, p->st),
+              "memcpy");
+      axpy_pert<R><<<(int)std::min<long long>((3 * p->g.sS * p->batch + 255) / 256, 4096), 256, 0, p->st>>>(
+          static_cast<C*>(S), P, p->g, p->F, p->batch, p->dtmp);
+      TG_CUDA(cudaGetLastError(), "axpy_pert");
+    }
+    TG_CUDA(cudaStreamSynchronize(p->st), "sync");
+    return TG_OK;
+  }
+};
+
+template <typename Fn>
+int dispatch(tg_plan* p, Fn&& fn) {
+  if (p->prec == TG_PREC_F64) return fn(Ops<double>());
+  return fn(Ops<float>());
+}
+
+int set_coefs(tg_plan* p, double dt, double nu, double eta) {
+  if (dt > 0.0 || nu >= 0.0) {
+    for (auto& c : p->hcoef) {
+      if (dt > 0.0) c.dt = dt;
+      if (nu >= 0.0) c.nu = nu;
+      if (eta >= 0.0) c.eta = eta;
+    }
+  }
+  TG_CUDA(cudaMemcpyAsync(p->coef, p->hcoef.data(), sizeof(RunCoef) * p->hcoef.size(), cudaMemcpyHostToDevice,
+                          p->st),
+          "coef upload");
+  return TG_OK;
+}
+
+void drop_graph(tg_plan* p) {
+  if (p->step_exec) cudaGraphExecDestroy(p->step_exec);
+  if (p->step_graph) cudaGraphDestroy(p->step_graph);
+  p->step_exec = nullptr;
+  p->step_graph = nullptr;
+  p->step_state = nullptr;
+}
+
+// advance nsteps RK4 steps; X must already hold the inverse-x fields of S
+int advance(tg_plan* p, void* S, int nsteps) {
+  if (nsteps <= 0) return TG_OK;
+  int rc;
+  int done = 0;
+  if (p->step_state != S || !p->step_exec) {
+    drop_graph(p);
+    // one eager step first: it also sets every kernel attribute outside capture
+    rc = dispatch(p, [&](auto ops) { return decltype(ops)::stages(p, S); });
+    if (rc) return rc;
+    done = 1;
+    TG_CUDA(cudaStreamBeginCapture(p->st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    const int64_t before = p->launches;
+    rc = dispatch(p, [&](auto ops) { return decltype(ops)::stages(p, S); });
+    p->launches = before;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(p->st, &graph);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "end capture");
+    e = cudaGraphInstantiate(&p->step_exec, graph, 0);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      return cuda_fail(e, "graph instantiate");
+    }
+    p->step_graph = graph;
+    p->step_state = S;
+  }
+  for (int s = done; s < nsteps; ++s) {
+    TG_CUDA(cudaGraphLaunch(p->step_exec, p->st), "graph launch");
+    p->launches += 16;
+  }
+  return TG_OK;
+}
+
+bool size_supported(int n, int prec) {
+  return prec == TG_PREC_F64 ? (find_f64(n) != nullptr) : (find_f32(n) != nullptr);
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+const char* tg_last_error(void) { return g_last_error.c_str(); }
+int tg_version(void) { return 100; }
+
+int tg_plan_create(tg_plan** out, const tg_desc* d) {
+  if (!out || !d) return fail(TG_E_INVALID, "tg_plan_create: null argument");
+  *out = nullptr;
+  if (d->physics != TG_PHYS_HYDRO && d->physics != TG_PHYS_MHD)
+    return fail(TG_E_INVALID, "tg_plan_create: physics must be TG_PHYS_HYDRO or TG_PHYS_MHD");
+  if (d->precision != TG_PREC_F32 && d->precision != TG_PREC_F64)
+    return fail(TG_E_INVALID, "tg_plan_create: precision must be TG_PREC_F32 or TG_PREC_F64");
+  if (d->batch < 1) return fail(TG_E_INVALID, "tg_plan_create: batch must be >= 1");
+  if (!size_supported(d->n, d->precision))
+    return fail(TG_E_UNSUPPORTED, "tg_plan_create: grid size " + std::to_string(d->n) +
+                                      " is not built for this precision");
+  const int n = d->n;
+  const int K = d->cutoff > 0 ? d->cutoff : n / 3;
+  if (K < 1 || K > n / 3)
+    return fail(TG_E_INVALID, "tg_plan_create: cutoff must satisfy 1 <= cutoff <= n/3 (2/3 rule)");
+  tg_plan* p = new (std::nothrow) tg_plan();
+  if (!p) return fail(TG_E_NOMEM, "tg_plan_create: host allocation failed");
+  p->n = n;
+  p->K = K;
+  p->batch = d->batch;
+  p->physics = d->physics;
+  p->prec = d->precision;
+  p->flags = d->flags;
+  p->F = d->physics == TG_PHYS_MHD ? 6 : 3;
+  p->G = 2 * p->F;
+  Geo& g = p->g;
+  g.n = n;
+  g.K = K;
+  g.M = 2 * K + 1;
+  g.Hk = K + 1;
+  g.Hz = (g.Hk + 3) / 4 * 4;
+  g.sS = (long long)g.M * g.M * g.Hz;
+  g.sX = (long long)n * g.M * g.Hz;
+  g.sY = (long long)n * n * g.Hz;
+  g.sP = (long long)n * n * n;
+  if (p->prec == TG_PREC_F64) p->l64 = find_f64(n);
+  else p->l32 = find_f32(n);
+  const size_t cs = csize(p);
+  const size_t B = (size_t)p->batch;
+  struct Alloc { void** ptr; size_t bytes; } allocs[] = {
+      {&p->X, cs * B * p->G * g.sX},
+      {&p->Y, cs * B * p->G * g.sY},
+      {&p->Z, cs * B * p->F * g.sY},
+      {&p->ACC, cs * B * p->F * g.sS},
+      {&p->VS, (p->flags & TG_FLAG_EXPLICIT_VISC) ? cs * B * p->F * g.sS : 0},
+      {&p->TW, cs * n},
+      {(void**)&p->part, sizeof(double) * B * kDiagBlocks * kNQ},
+      {(void**)&p->dtmp, sizeof(double) * B * TG_DIAG_WIDTH},
+      {(void**)&p->amax, sizeof(unsigned long long) * B * 6},
+      {(void**)&p->coef, sizeof(RunCoef) * B},
+  };
+  for (auto& a : allocs) {
+    if (a.bytes == 0) continue;
+    cudaError_t e = cudaMalloc(a.ptr, a.bytes);
+    if (e != cudaSuccess) {
+      tg_plan_destroy(p);
+      return fail(TG_E_NOMEM, std::string("tg_plan_create: cudaMalloc failed: ") + cudaGetErrorString(e));
+    }
+    p->scratch += (int64_t)a.bytes;
+  }
+  // twiddles W_N^m = exp(-2 pi i m / N), generated in FP64
+  std::vector<double> tw(2 * (size_t)n);
+  for (int m = 0; m < n; ++m) {
+    // exact quarter-turn values; cos/sin of a reduced angle elsewhere
+    const double ang = 2.0 * M_PI * (double)m / (double)n;
+    double c = std::cos(ang), s = std::sin(ang);
+    if ((4 * m) % n == 0) {
+      const int q = (4 * m) / n;
+      c = (q == 0) ? 1.0 : (q == 2 ? -1.0 : 0.0);
+      s = (q == 1) ? 1.0 : (q == 3 ? -1.0 : 0.0);
+    }
+    tw[2 * m] = c;
+    tw[2 * m + 1] = -s;
+  }
+  cudaError_t e;
+  if (p->prec == TG_PREC_F64) {
+    e = cudaMemcpy(p->TW, tw.data(), sizeof(double) * 2 * n, cudaMemcpyHostToDevice);
+  } else {
+    std::vector<float> tf(tw.begin(), tw.end());
+    e = cudaMemcpy(p->TW, tf.data(), sizeof(float) * 2 * n, cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) {
+    tg_plan_destroy(p);
+    return cuda_fail(e, "tg_plan_create: twiddle upload");
+  }
+  p->hcoef.assign(p->batch, RunCoef{0.0, 0.0, 0.0, (p->flags & TG_FLAG_LORENTZ_REF) ? -1.0 : 1.0});
+  e = cudaMemcpy(p->coef, p->hcoef.data(), sizeof(RunCoef) * p->batch, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(p->amax, 0, sizeof(unsigned long long) * B * 6);
+  if (e != cudaSuccess) {
+    tg_plan_destroy(p);
+    return cuda_fail(e, "tg_plan_create: init");
+  }
+  *out = p;
+  return TG_OK;
+}
+
+int tg_plan_destroy(tg_plan* p) {
+  if (!p) return TG_OK;
+  drop_graph(p);
+  void* bufs[] = {p->X, p->Y, p->Z, p->ACC, p->VS, p->TW, p->part, p->dtmp, p->amax, p->coef};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  delete p;
+  return TG_OK;
+}
+
+int tg_set_stream(tg_plan* p, void* stream) {
+  if (!p) return fail(TG_E_INVALID, "tg_set_stream: null plan");
+  if (p->st != static_cast<cudaStream_t>(stream)) drop_graph(p);
+  p->st = static_cast<cudaStream_t>(stream);
+  return TG_OK;
+}
+
+int64_t tg_state_layout(const tg_plan* p, int dims[7]) {
+  if (!p) return 0;
+  if (dims) {
+    dims[0] = p->batch;
+    dims[1] = p->F;
+    dims[2] = p->g.M;
+    dims[3] = p->g.M;
+    dims[4] = p->g.Hz;
+    dims[5] = p->K;
+    dims[6] = p->n;
+  }
+  return (int64_t)p->batch * p->F * p->g.sS;
+}
+
+int64_t tg_plan_scratch_bytes(const tg_plan* p) { return p ? p->scratch : 0; }
+int64_t tg_last_launch_count(const tg_plan* p) { return p ? p->launches : 0; }
+
+int tg_set_run_params(tg_plan* p, const double* nu, const double* eta, const double* dt, int count) {
+  if (!p) return fail(TG_E_INVALID, "tg_set_run_params: null plan");
+  if (count != 1 && count != p->batch) return fail(TG_E_INVALID, "tg_set_run_params: count must be 1 or batch");
+  for (int r = 0; r < p->batch; ++r) {
+    const int i = (count == 1) ? 0 : r;
+    if (nu) {
+      if (!(nu[i] >= 0.0)) return fail(TG_E_INVALID, "tg_set_run_params: nu must be nonnegative");
+      p->hcoef[r].nu = nu[i];
+    }
+    if (eta) {
+      if (!(eta[i] >= 0.0)) return fail(TG_E_INVALID, "tg_set_run_params: eta must be nonnegative");
+      p->hcoef[r].eta = eta[i];
+    }
+    if (dt) {
+      if (!(dt[i] > 0.0)) return fail(TG_E_INVALID, "tg_set_run_params: dt must be positive");
+      p->hcoef[r].dt = dt[i];
+    }
+  }
+  return set_coefs(p, -1.0, -1.0, -1.0);
+}
+
+int tg_initial_condition(tg_plan* p, int kind, uint64_t seed, double pert_amp, double k0, double b_amp,
+                         void* state) {
+  if (!p || !state) return fail(TG_E_INVALID, "tg_initial_condition: null argument");
+  if (kind < TG_IC_TAYLOR_GREEN || kind > TG_IC_ZERO) return fail(TG_E_INVALID, "tg_initial_condition: bad kind");
+  if ((kind == TG_IC_MHD_REFERENCE || kind == TG_IC_MHD_EQUAL_ENERGY) && p->F != 6)
+    return fail(TG_E_INVALID, "tg_initial_condition: MHD initial condition needs an MHD plan");
+  if (pert_amp < 0.0 || (pert_amp > 0.0 && !(k0 > 0.0)))
+    return fail(TG_E_INVALID, "tg_initial_condition: need pert_amp >= 0 and k0 > 0");
+  p->launches = 0;
+  return dispatch(p, [&](auto ops) { return decltype(ops)::initial(p, kind, seed, pert_amp, k0, b_amp, state); });
+}
+
+int tg_forward(tg_plan* p, const void* phys, void* state) {
+  if (!p || !phys || !state) return fail(TG_E_INVALID, "tg_forward: null argument");
+  p->launches = 0;
+  return dispatch(p, [&](auto ops) {
+    using O = decltype(ops);
+    int rc;
+    if ((rc = O::z_r2c(p, phys, p->F))) return rc;
+    if ((rc = O::y_fwd(p, p->F))) return rc;
+    return O::x_fwd(p, state, nullptr, false);
+  });
+}
+
+int tg_inverse(tg_plan* p, const void* state, void* phys) {
+  if (!p || !phys || !state) return fail(TG_E_INVALID, "tg_inverse: null argument");
+  p->launches = 0;
+  return dispatch(p, [&](auto ops) {
+    using O = decltype(ops);
+    int rc;
+    if ((rc = O::load_inv(p, state, MAP_ID, p->F, p->F))) return rc;
+    if ((rc = O::y_inv(p, p->F))) return rc;
+    return O::z_c2r(p, phys, p->F, false);
+  });
+}
+
+int tg_rhs(tg_plan* p, const void* state, double nu, double eta, void* rhs_out) {
+  if (!p || !state || !rhs_out) return fail(TG_E_INVALID, "tg_rhs: null argument");
+  int rc = set_coefs(p, -1.0, nu, eta);
+  if (rc) return rc;
+  p->launches = 0;
+  return dispatch(p, [&](auto ops) {
+    using O = decltype(ops);
+    int r;
+    if ((r = O::start(p, state))) return r;
+    if ((r = O::y_inv(p, p->G))) return r;
+    if ((r = O::z_prod(p))) return r;
+    if ((r = O::y_fwd(p, p->F))) return r;
+    return O::x_fwd(p, rhs_out, state, true);
+  });
+}
+
+int tg_step(tg_plan* p, void* state, double dt, double nu, double eta, int nsteps) {
+  if (!p || !state) return fail(TG_E_INVALID, "tg_step: null argument");
+  if (nsteps < 0) return fail(TG_E_INVALID, "tg_step: nsteps must be >= 0");
+  if (dt > 0.0 && nu < 0.0) return fail(TG_E_INVALID, "tg_step: nu must be nonnegative");
+  int rc = set_coefs(p, dt, nu, eta);
+  if (rc) return rc;
+  for (const auto& c : p->hcoef)
+    if (!(c.dt > 0.0)) return fail(TG_E_INVALID, "tg_step: dt must be positive");
+  p->launches = 0;
+  if (nsteps == 0) return TG_OK;
+  rc = dispatch(p, [&](auto ops) { return decltype(ops)::start(p, state); });
+  if (rc) return rc;
+  return advance(p, state, nsteps);
+}
+
+int tg_run(tg_plan* p, void* state, double dt, double nu, double eta, int nsteps, int save_every,
+           double* series) {
+  if (!p || !state || !series) return fail(TG_E_INVALID, "tg_run: null argument");
+  if (nsteps < 0 || save_every < 1) return fail(TG_E_INVALID, "tg_run: need nsteps >= 0 and save_every >= 1");
+  int rc = set_coefs(p, dt, nu, eta);
+  if (rc) return rc;
+  for (const auto& c : p->hcoef)
+    if (!(c.dt > 0.0)) return fail(TG_E_INVALID, "tg_run: dt must be positive");
+  p->launches = 0;
+  const long long stride = (long long)p->batch * TG_DIAG_WIDTH;
+  int64_t total = 0;
+  rc = dispatch(p, [&](auto ops) { return decltype(ops)::diagnostics(p, state, series); });
+  if (rc) return rc;
+  total += p->launches;
+  int rec = 1;
+  int step = 0;
+  while (step < nsteps) {
+    const int chunk = std::min(save_every - (step % save_every), nsteps - step);
+    p->launches = 0;
+    rc = dispatch(p, [&](auto ops) { return decltype(ops)::start(p, state); });
+    if (rc) return rc;
+    rc = advance(p, state, chunk);
+    if (rc) return rc;
+    step += chunk;
+    rc = dispatch(p, [&](auto ops) { return decltype(ops)::diagnostics(p, state, series + rec * stride); });
+    if (rc) return rc;
+    total += p->launches;
+    ++rec;
+  }
+  p->launches = total;
+  return TG_OK;
+}
+
+int tg_diagnostics(tg_plan* p, const void* state, double nu, double eta, double* out) {
+  if (!p || !state || !out) return fail(TG_E_INVALID, "tg_diagnostics: null argument");
+  int rc = set_coefs(p, -1.0, nu, eta);
+  if (rc) return rc;
+  p->launches = 0;
+  return dispatch(p, [&](auto ops) { return decltype(ops)::diagnostics(p, state, out); });
+}
+
+int tg_field_absmax(tg_plan* p, const void* state, int which, double* out) {
+  if (!p || !state || !out) return fail(TG_E_INVALID, "tg_field_absmax: null argument");
+  if (which != TG_ABSMAX_VELOCITY && which != TG_ABSMAX_DIVERGENCE)
+    return fail(TG_E_INVALID, "tg_field_absmax: bad selector");
+  p->launches = 0;
+  return dispatch(p, [&](auto ops) { return decltype(ops)::absmax(p, state, which, out); });
+}
+
+int tg_derived(tg_plan* p, const void* state, int which, void* phys) {
+  if (!p || !state || !phys) return fail(TG_E_INVALID, "tg_derived: null argument");
+  if (which != TG_DERIVED_VORTICITY && which != TG_DERIVED_DIVERGENCE)
+    return fail(TG_E_INVALID, "tg_derived: bad selector");
+  p->launches = 0;
+  return dispatch(p, [&](auto ops) { return decltype(ops)::derived(p, state, which, phys); });
+}
+
+int tg_to_full_spectrum(tg_plan* p, const void* state, void* full) {
+  if (!p || !state || !full) return fail(TG_E_INVALID, "tg_to_full_spectrum: null argument");
+  p->launches = 0;
+  return dispatch(p, [&](auto ops) { return decltype(ops)::full(p, state, full, true); });
+}
+
+int tg_from_full_spectrum(tg_plan* p, const void* full, void* state) {
+  if (!p || !state || !full) return fail(TG_E_INVALID, "tg_from_full_spectrum: null argument");
+  p->launches = 0;
+  return dispatch(p, [&](auto ops) { return decltype(ops)::full(p, full, state, false); });
+}
+
+int tg_physical_energy(tg_plan* p, const void* phys, double* out) {
+  if (!p || !phys || !out) return fail(TG_E_INVALID, "tg_physical_energy: null argument");
+  p->launches = 0;
+  return dispatch(p, [&](auto ops) { return decltype(ops)::energy(p, phys, out); });
+}
+
+}  // extern "C"

@@ -1,0 +1,106 @@
+// Shared definitions of the Taylor-Green pseudo-spectral kernels: geometry of
+// the pruned half-spectrum layouts, per-size FFT plans and kernel arguments.
+//
+// Layouts (complex, kz innermost with a padded row stride Hz):
+//   state S, accumulator A   [run][F][M][M][Hz]   kept modes only (compact)
+//   X  (after inverse-x)     [run][G][N][M][Hz]   x physical, ky kept
+//   Y  (after inverse-y)     [run][G][N][N][Hz]   x, y physical
+//   Z  (forward-z output)    [run][F][N][N][Hz]
+//   W  (after forward-y)     [run][F][N][M][Hz]   (aliases Y)
+// with K the 2/3 cutoff, M = 2K+1 kept modes on a full axis (ordered
+// 0..K, -K..-1), Hk = K+1 kept kz modes, F = 3 (hydro) or 6 (MHD) state
+// fields and G = 2F transformed fields (u, curl u [, b, curl b]).
+// Spectral values are Fourier coefficients: u(x) = sum_k c_k exp(i k.x).
+#pragma once
+
+#include <cstdint>
+
+#include "tg_fft.cuh"
+
+namespace tg {
+
+struct Geo {
+  int n, K, M, Hk, Hz;
+  long long sS;  // complex elements per field, compact state: M*M*Hz
+  long long sX;  // per field of X / W: N*M*Hz
+  long long sY;  // per field of Y / Z: N*N*Hz
+  long long sP;  // real elements per physical field: N^3
+};
+
+struct RunCoef {
+  double nu, eta, dt;
+  double lorentz;  // sign of j x b in the momentum equation (+1 physical)
+};
+
+// per-size FFT plan (radix sequence and threads per transform)
+template <int N> struct PlanFor;
+template <> struct PlanFor<8> { using T = FftPlan<8, 2, 4, 2>; };
+template <> struct PlanFor<12> { using T = FftPlan<12, 1, 4, 3>; };
+template <> struct PlanFor<16> { using T = FftPlan<16, 4, 4, 4>; };
+template <> struct PlanFor<24> { using T = FftPlan<24, 2, 2, 12>; };
+template <> struct PlanFor<32> { using T = FftPlan<32, 4, 8, 4>; };
+template <> struct PlanFor<48> { using T = FftPlan<48, 4, 4, 12>; };
+template <> struct PlanFor<64> { using T = FftPlan<64, 8, 8, 8>; };
+template <> struct PlanFor<96> { using T = FftPlan<96, 4, 8, 12>; };
+template <> struct PlanFor<128> { using T = FftPlan<128, 8, 16, 8>; };
+template <> struct PlanFor<256> { using T = FftPlan<256, 16, 16, 16>; };
+template <> struct PlanFor<512> { using T = FftPlan<512, 16, 16, 32>; };
+
+__host__ __device__ constexpr int kept_of(int n) { return n / 3; }
+
+// columns (consecutive kz) per CTA of the x and y passes
+template <typename R, int N, int F> struct TileZ {
+  static constexpr int base = (N >= 128) ? 16 : ((N >= 12) ? 8 : 4);
+  static constexpr int CS = ColLayout<N>::CS;
+  static constexpr long long smem(int tz) {
+    // twiddles + exchange columns + spectral column buffer (F fields, M <= 2*(N/3)+1 rows)
+    return (long long)sizeof(cplx<R>) * (N + tz * CS + (long long)F * (2 * (N / 3) + 1) * tz);
+  }
+  static constexpr int value = (smem(base) <= 200 * 1024) ? base : base / 2;
+};
+
+// line pairs per CTA of the z pass
+template <typename R, int N> struct LinesZ {
+  static constexpr int P = PlanFor<N>::T::P;
+  static constexpr int pref = (P >= 16) ? 8 : ((P >= 8) ? 16 : 32);
+  static constexpr int pairs = N * N / 2;
+  // largest power of two <= pref dividing the number of line pairs
+  static constexpr int value = (pairs % pref == 0) ? pref
+      : (pairs % (pref / 2) == 0) ? pref / 2 : (pairs % (pref / 4) == 0) ? pref / 4 : 1;
+};
+
+enum KxMode { KX_STAGE = 0, KX_LOAD = 1, KX_FWD = 2 };
+enum FieldMap { MAP_ID = 0, MAP_UW = 1, MAP_UWBJ = 2, MAP_DIV = 3, MAP_DIVB = 4, MAP_CURL = 5 };
+enum KzMode { KZ_PROD_HD = 0, KZ_PROD_MHD = 1, KZ_C2R = 2, KZ_R2C = 3 };
+enum Flags { FLAG_EXPLICIT = 1, FLAG_RHS = 2, FLAG_AMAX = 4 };
+
+template <typename R> struct PassArgs {
+  Geo g;
+  const cplx<R>* in;     // pass input (X, Y, Z or W)
+  cplx<R>* out;          // pass output
+  cplx<R>* S;            // state (KX_STAGE)
+  cplx<R>* acc;          // RK4 accumulator
+  cplx<R>* vs;           // stage state (explicit-viscosity RK4 only)
+  const cplx<R>* spec_in;
+  cplx<R>* spec_out;
+  const R* phys_in;
+  R* phys_out;
+  const cplx<R>* tw;     // W_N^m, forward sign
+  const RunCoef* coef;   // per run
+  unsigned long long* amax;  // per (run, field) abs-max bit patterns
+  int stage;             // 1..4
+  int flags;
+  int map;               // FieldMap for KX_LOAD
+  int nin, nout;         // fields read / written by this pass
+};
+
+// signed wavenumber of compact index i (0..M-1)
+__device__ __forceinline__ int ksigned(int i, int K) { return i <= K ? i : i - (2 * K + 1); }
+// compact index of full-axis frequency row k, or -1 when k is dealiased away
+__device__ __forceinline__ int kcompact(int k, int N, int K) {
+  return k <= K ? k : (k >= N - K ? k - N + 2 * K + 1 : -1);
+}
+// full-axis frequency row of compact index i
+__device__ __forceinline__ int kfull(int i, int N, int K) { return i <= K ? i : i + N - (2 * K + 1); }
+
+}  // namespace tg

@@ -1,0 +1,210 @@
+// In-register DFT codelets and the shared-memory Stockham pass engine used by
+// every transform pass of the Taylor-Green time step.
+//
+// A length-N transform is executed by P cooperating threads ("one column").
+// It is a sequence of radix-R passes (N = R_0 * R_1 * ...), each thread doing
+// N/(R*P) radix-R butterflies per pass, in the self-sorting Stockham order of
+// Govindaraju et al. (SC 2008): pass with sub-length Ns reads
+// x[j + r*N/R], multiplies by W_{Ns*R}^{(j mod Ns) r}, does a radix-R DFT and
+// writes y[(j/Ns)*Ns*R + (j mod Ns) + r*Ns].  The first pass reads through a
+// caller functor (global memory, Hermitian packing, a spectral formula ...),
+// the last pass hands each result to a caller functor; intermediate data sit
+// in a padded shared-memory column.  Twiddles W_N^m come from a table
+// generated in FP64 on the host.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "tg_consts.cuh"
+
+namespace tg {
+
+// ------------------------------------------------------------------ complex
+template <typename R> struct CplxT;
+template <> struct CplxT<float> { using T = float2; };
+template <> struct CplxT<double> { using T = double2; };
+template <typename R> using cplx = typename CplxT<R>::T;
+
+template <typename C> __device__ __forceinline__ C mk(decltype(C::x) a, decltype(C::x) b) {
+  C c; c.x = a; c.y = b; return c;
+}
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return mk<C>(a.x + b.x, a.y + b.y); }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { return mk<C>(a.x - b.x, a.y - b.y); }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+  return mk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+template <typename C> __device__ __forceinline__ C cmulc(C a, C b) {
+  return mk<C>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+template <typename C> __device__ __forceinline__ C cscale(C a, decltype(C::x) s) { return mk<C>(a.x * s, a.y * s); }
+template <typename C> __device__ __forceinline__ C cconj(C a) { return mk<C>(a.x, -a.y); }
+// multiply by i*s (s = +1 or -1 at compile time, or any real)
+template <typename C> __device__ __forceinline__ C cmul_i(C a) { return mk<C>(-a.y, a.x); }
+template <typename C> __device__ __forceinline__ C czero() { return mk<C>(0, 0); }
+
+// W_R^m with sign DIR (-1 forward, +1 inverse), R | 96, folded at compile time
+template <typename C, int R, int DIR>
+__device__ __forceinline__ C wconst(int m) {
+  using Re = decltype(C::x);
+  const int q = (m % R) * (96 / R);
+  return mk<C>(Re(kCos96(q)), Re(DIR * kSin96(q)));
+}
+
+// ------------------------------------------------------------------ codelets
+template <int R> struct Split {
+  static constexpr int A = (R % 4 == 0 && R > 4) ? 4 : ((R % 2 == 0 && R > 2) ? 2 : ((R % 3 == 0 && R > 3) ? 3 : R));
+  static constexpr int B = R / A;
+};
+
+// In-place DFT of R values held in registers: X[k] = sum_n x[n] W_R^{nk},
+// W_R = exp(DIR * 2 pi i / R).
+template <int R, int DIR, typename C>
+__device__ __forceinline__ void dft(C* v) {
+  using Re = decltype(C::x);
+  if constexpr (R == 1) {
+  } else if constexpr (R == 2) {
+    C a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  } else if constexpr (R == 3) {
+    const Re h = Re(0.5), s = Re(DIR * 0.8660254037844386);  // sin(2 pi / 3)
+    C a = v[0], b = v[1], c = v[2];
+    C t1 = cadd(b, c);
+    C t2 = mk<C>(a.x - h * t1.x, a.y - h * t1.y);
+    C d = csub(b, c);
+    C t3 = mk<C>(-s * d.y, s * d.x);  // i * s * (b - c)
+    v[0] = cadd(a, t1);
+    v[1] = cadd(t2, t3);
+    v[2] = csub(t2, t3);
+  } else if constexpr (R == 4) {
+    C a = v[0], b = v[1], c = v[2], d = v[3];
+    C s0 = cadd(a, c), s1 = csub(a, c), s2 = cadd(b, d), s3 = csub(b, d);
+    // i*DIR*(b-d)
+    C r3 = (DIR > 0) ? mk<C>(-s3.y, s3.x) : mk<C>(s3.y, -s3.x);
+    v[0] = cadd(s0, s2);
+    v[1] = cadd(s1, r3);
+    v[2] = csub(s0, s2);
+    v[3] = csub(s1, r3);
+  } else {
+    constexpr int A = Split<R>::A, B = Split<R>::B;
+    C t[R];
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) {
+      C a[A];
+#pragma unroll
+      for (int n1 = 0; n1 < A; ++n1) a[n1] = v[B * n1 + n2];
+      dft<A, DIR>(a);
+#pragma unroll
+      for (int k1 = 0; k1 < A; ++k1) {
+        if (n2 * k1 == 0) {
+          t[n2 * A + k1] = a[k1];
+        } else {
+          t[n2 * A + k1] = cmul(a[k1], wconst<C, R, DIR>(n2 * k1));
+        }
+      }
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) {
+      C b[B];
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) b[n2] = t[n2 * A + k1];
+      dft<B, DIR>(b);
+#pragma unroll
+      for (int k2 = 0; k2 < B; ++k2) v[k1 + A * k2] = b[k2];
+    }
+  }
+}
+
+// ------------------------------------------------------------------ plans
+// N = product of the radices; P threads per transform.
+template <int N_, int P_, int R0_, int R1_ = 1, int R2_ = 1>
+struct FftPlan {
+  static constexpr int N = N_, P = P_;
+  static constexpr int NPASS = (R1_ == 1) ? 1 : ((R2_ == 1) ? 2 : 3);
+  template <int I> __host__ __device__ static constexpr int radix() { return I == 0 ? R0_ : (I == 1 ? R1_ : R2_); }
+  static_assert(R0_ * R1_ * R2_ == N_, "radices must multiply to N");
+  static_assert((N_ / R0_) % P_ == 0 && (N_ / R1_) % P_ == 0 && (N_ / R2_) % P_ == 0,
+                "P must divide N/R for every pass");
+  static constexpr int E = N_ / P_;  // elements held per thread per pass
+};
+
+// padded shared-memory index: one spare slot every 16 complex values
+__device__ __forceinline__ int padx(int n) { return n + (n >> 4); }
+template <int N> struct ColLayout {
+  // per-column stride in complex elements (odd, so that columns interleave banks)
+  static constexpr int PADN = N + (N >> 4);
+  static constexpr int CS = (PADN % 2 == 0) ? PADN + 1 : PADN;
+};
+
+// Execute pass I of Plan for one column.
+//   src(n)            -> value at input index n (pass 0 only)
+//   dst(b, r, k, v)   <- output v at index k (last pass); b, r compile-time
+//   xb                -> this column's padded shared-memory buffer
+//   tw                -> table W_N^m (forward sign), shared or global
+// All threads of the CTA must call this together (it contains __syncthreads).
+template <class Plan, int DIR, int I, int NS, typename C, class Src, class Dst>
+__device__ __forceinline__ void fft_pass(int t, Src& src, Dst& dst, C* xb, const C* tw) {
+  constexpr int N = Plan::N, P = Plan::P;
+  constexpr int R = Plan::template radix<I>();
+  constexpr int NB = N / (R * P);
+  constexpr bool LAST = (I == Plan::NPASS - 1);
+  C v[NB][R];
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    const int j = t + P * b;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      if constexpr (I == 0) {
+        v[b][r] = src(j + r * (N / R));
+      } else {
+        v[b][r] = xb[padx(j + r * (N / R))];
+      }
+    }
+    if constexpr (I > 0) {
+      const int jm = j % NS;
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        C w = tw[jm * r * (N / (NS * R))];
+        if constexpr (DIR > 0) w.y = -w.y;
+        v[b][r] = cmul(v[b][r], w);
+      }
+    }
+    dft<R, DIR>(v[b]);
+  }
+  if constexpr (!LAST) {
+    __syncthreads();  // every reader of xb (this or a previous transform) is done
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int j = t + P * b;
+      const int jm = j % NS;
+      const int base = (j / NS) * NS * R + jm;
+#pragma unroll
+      for (int r = 0; r < R; ++r) xb[padx(base + r * NS)] = v[b][r];
+    }
+    __syncthreads();
+    fft_pass<Plan, DIR, I + 1, NS * R>(t, src, dst, xb, tw);
+  } else {
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int j = t + P * b;
+#pragma unroll
+      for (int r = 0; r < R; ++r) dst(b, r, j + r * NS, v[b][r]);
+    }
+  }
+}
+
+template <class Plan, int DIR, typename C, class Src, class Dst>
+__device__ __forceinline__ void fft_column(int t, Src& src, Dst& dst, C* xb, const C* tw) {
+  fft_pass<Plan, DIR, 0, 1>(t, src, dst, xb, tw);
+}
+
+// index of output element (b, r) held by thread t after the last pass
+template <class Plan>
+__device__ __forceinline__ int out_index(int t, int b, int r) {
+  constexpr int R = Plan::template radix<Plan::NPASS - 1>();
+  constexpr int NS = Plan::N / R;
+  return t + Plan::P * b + r * NS;
+}
+
+}  // namespace tg

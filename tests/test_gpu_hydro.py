@@ -1,0 +1,111 @@
+"""Hydro RHS, RK4 step and run loop on the GPU against the reference fixtures.
+
+Fixtures come from the reference's own jax/taylor_green_jax.py (see
+tests/golden/make_golden.py).  Tolerances: FP32 kernels 1e-5 relative L2 on
+fields and 1e-6 relative on diagnostics (the parity bar of the hot path);
+FP64 kernels 1e-12.
+"""
+import numpy as np
+import pytest
+
+from conftest import from_state, rel_l2, to_state, unpack_sparse
+from oracle import tg_numpy as T
+
+pytestmark = pytest.mark.gpu
+
+
+def _plan(N, prec="f32", **kw):
+    import jax_tg_project_gb300 as tg
+    return tg.Plan(N, precision=prec, **kw)
+
+
+def _phys_to_state(p, u):
+    import torch
+    return p.forward(torch.from_numpy(np.asarray(u)[None]).to(p.real_dtype).cuda().contiguous())
+
+
+@pytest.mark.parametrize("prec,tol", [("f32", 1e-5), ("f64", 1e-12)])
+def test_rhs_matches_reference(golden_hydro, prec, tol):
+    g = golden_hydro
+    p = _plan(16, prec)
+    s = _phys_to_state(p, g["rhs16_in"])
+    r = p.rhs(s, nu=0.01)
+    got = p.inverse(r)[0].double().cpu().numpy()
+    assert rel_l2(got, g["rhs16_out"]) < tol
+
+
+def test_zero_mode_is_not_damped():  # jax/test_taylor_green_jax.py:45-51
+    p = _plan(8, "f64")
+    s = _phys_to_state(p, np.ones((3, 8, 8, 8)))
+    r = p.inverse(p.rhs(s, nu=0.01))[0].cpu().numpy()
+    assert np.abs(r).max() < 1e-12
+
+
+@pytest.mark.parametrize("prec,explicit,tol", [("f32", False, 1e-5), ("f32", True, 1e-5),
+                                               ("f64", False, 1e-9), ("f64", True, 1e-12)])
+def test_step_matches_reference(golden_hydro, prec, explicit, tol):
+    g = golden_hydro
+    p = _plan(16, prec, explicit_viscosity=explicit)
+    s = _phys_to_state(p, g["rhs16_in"])
+    p.step(s, dt=0.005, nu=0.01, nsteps=1)
+    got = p.inverse(s)[0].double().cpu().numpy()
+    assert rel_l2(got, g["step16_out"]) < tol
+
+
+@pytest.mark.parametrize("case,N,nu,nsteps", [("run8", 8, 0.01, 4), ("run16", 16, 2 * np.pi / 100, 10)])
+def test_run_series_matches_reference(golden_hydro, case, N, nu, nsteps):
+    g = golden_hydro
+    for prec, tol in (("f32", 1e-6), ("f64", 1e-12)):
+        p = _plan(N, prec, explicit_viscosity=True)
+        s = p.initial_condition("taylor_green")
+        series = p.run(s, dt=0.005, nu=nu, nsteps=nsteps, save_every=2).cpu().numpy()[:, 0]
+        np.testing.assert_allclose(series[:, 0], g[f"{case}_energy"], rtol=tol)
+        np.testing.assert_allclose(series[:, 1], g[f"{case}_enstrophy"], rtol=tol)
+        np.testing.assert_allclose(series[:, 2], g[f"{case}_dissipation"], rtol=tol)
+        assert series[:, 6].max() < (1e-5 if prec == "f32" else 1e-10)
+        u = p.inverse(s)[0].double().cpu().numpy()
+        assert rel_l2(u, g[f"{case}_u"]) < (1e-6 if prec == "f32" else 1e-12)
+
+
+def test_tg64_100_steps_velocity_parity(golden_tg64):
+    """The parity bar: 64^3, nu=1/1600, dt=1e-3, 100 steps, FP32 kernels vs FP64 reference."""
+    c100 = unpack_sparse(golden_tg64, "c100")
+    for explicit in (False, True):
+        p = _plan(64, "f32", explicit_viscosity=explicit)
+        s = p.initial_condition("taylor_green")
+        p.step(s, dt=1e-3, nu=1 / 1600, nsteps=100)
+        err = rel_l2(from_state(p, s)[0], c100)
+        assert err < 1e-5, err
+
+
+def test_tg64_series_parity(golden_tg64):
+    g = golden_tg64
+    p = _plan(64, "f32")
+    s = p.initial_condition("taylor_green")
+    series = p.run(s, dt=1e-3, nu=1 / 1600, nsteps=200, save_every=10).cpu().numpy()[:, 0]
+    for col, key in ((0, "energy"), (1, "enstrophy"), (2, "dissipation")):
+        np.testing.assert_allclose(series[:, col], g[f"series_{key}"], rtol=1e-6)
+    assert rel_l2(from_state(p, s)[0], unpack_sparse(g, "c200")) < 1e-5
+    assert all(a >= b for a, b in zip(series[:, 0], series[1:, 0]))  # energy decays
+
+
+def test_fp64_tracks_reference_to_roundoff(golden_tg64):
+    p = _plan(64, "f64", explicit_viscosity=True)
+    s = p.initial_condition("taylor_green")
+    p.step(s, dt=1e-3, nu=1 / 1600, nsteps=100)
+    assert rel_l2(from_state(p, s)[0], unpack_sparse(golden_tg64, "c100")) < 1e-12
+
+
+def test_batched_runs_are_independent():
+    """A batch of runs with different nu equals the runs done one at a time."""
+    import torch
+    nus = [0.01, 0.002, 0.0005]
+    pb = _plan(32, "f32", batch=3)
+    sb = pb.initial_condition("taylor_green", seed=3, pert_amp=1e-2, k0=4.0)
+    pb.set_run_params(nu=nus, eta=[0.0] * 3, dt=[2e-3] * 3)
+    pb.step(sb, nsteps=5)
+    for r, nu in enumerate(nus):
+        p1 = _plan(32, "f32")
+        s1 = p1.initial_condition("taylor_green", seed=3 + r, pert_amp=1e-2, k0=4.0)
+        p1.step(s1, dt=2e-3, nu=nu, nsteps=5)
+        assert torch.equal(s1[0], sb[r])
