@@ -1,0 +1,335 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300-native Taylor-Green time step.
+
+Workload (the single-GPU throughput configuration): plain hydro Taylor-Green on
+256^3, FP32 fields with FP64 reductions, nu = 1/1600, RK4 dt = 2.5e-4.  One
+"step" is one RK4 step (4 stages x 4 pass kernels).  Inputs are larger than L2
+(state + scratch ~ 0.7 GB), so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints ONE JSON line (rank 0).  Under torchrun (N > 1) every rank advances an
+independent replica (the path does not shard); ``value`` is the sum of steps/s.
+``--impl reference`` times the reference's CPU algorithm (the NumPy FP64
+restatement in oracle/, JAX being unavailable) on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "RK4 steps/s at 256^3 FP32"
+UNIT = "steps/s"
+N_GRID = 256
+NU = 1.0 / 1600.0
+DT = 2.5e-4
+SAVE_EVERY = 10
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--n", type=int, default=N_GRID)
+    ap.add_argument("--cpu-budget", type=float, default=30.0,
+                    help="seconds of host time for the CPU legs")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------- helpers
+def algorithmic_bytes(n, K=None, F=3, csize=8):
+    """Bytes each pass must move per launch (kept modes only, padding excluded)."""
+    K = n // 3 if K is None else K
+    M, Hk, G = 2 * K + 1, K + 1, 2 * F
+    X = n * M * Hk * csize   # one field after inverse-x / forward-y
+    Y = n * n * Hk * csize   # one field after inverse-y / forward-z
+    S = M * M * Hk * csize   # one compact spectral field
+    return {
+        "ky_inverse": G * (X + Y),
+        "kz_product_hd" if F == 3 else "kz_product_mhd": G * Y + F * Y,
+        "ky_forward": F * (Y + X),
+        # stages 2-3 (read W, S, acc; write acc, X); stage 1 skips the acc read,
+        # stage 4 writes S instead of acc: the mean over the 4 stages
+        "kx_stage_hd" if F == 3 else "kx_stage_mhd": F * X + F * S + 0.75 * F * S + F * S + G * X,
+    }
+
+
+def step_bytes(n, F=3, csize=8):
+    b = algorithmic_bytes(n, F=F, csize=csize)
+    return 4 * sum(b.values())
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of a pass kernel from the committed ncu summary, or None."""
+    p = os.path.join(HERE, "profiles", "dram_bytes_256.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for ln in f:
+            parts = ln.split()
+            if len(parts) >= 2 and parts[0] == kernel:
+                try:
+                    return float(parts[1])
+                except ValueError:
+                    return None
+    return None
+
+
+def cpu_step_seconds(n, budget):
+    """Wall time of RK4 steps of the reference algorithm (NumPy/SciPy FP64 restatement)."""
+    from oracle import tg_numpy as T
+
+    T.WORKERS = -1
+    kx, ky, kz = T.make_wavenumbers(n)
+    mask = T.make_dealias_mask(n)
+    u = T.initial_taylor_green(n)
+    times = []
+    t_start = time.perf_counter()
+    while True:
+        t0 = time.perf_counter()
+        u = T.advance_one_step(u, DT, NU, kx, ky, kz, mask)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_start + times[-1] > budget or len(times) >= 50:
+            break
+    return times
+
+
+# ---------------------------------------------------------------------- arms
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    n = args.n
+    cores = os.cpu_count() or 1
+    # warm-up: one step (first-touch of the FFT plans and buffers), then timed steps
+    budget = args.cpu_budget
+    warm = cpu_step_seconds(n, budget=0.0) if args.warmup > 0 else []
+    times = cpu_step_seconds(n, budget=max(budget - sum(warm), 1.0))
+    times = times[: max(1, min(args.steps, len(times)))]
+    v = len(times) / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+        "steps": len(times), "warmup": len(warm), "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": f"taylor_green_hydro_{n}^3", "n": n, "nu": NU,
+                                         "dt": DT},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{len(times)} RK4 step(s) at {n}^3 of the reference JAX "
+                                   "algorithm restated in NumPy/SciPy FP64 (jax is not installed); "
+                                   f"FFTs on {cores} threads"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    import jax_tg_project_gb300 as tg
+
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    n = args.n
+    W = max(3, args.warmup)
+    K = args.steps
+    plan = tg.Plan(n, precision="f32", device=dev)
+    state = plan.initial_condition("taylor_green")
+    init_host = state.to("cpu").pin_memory()
+    plan.step(state, dt=DT, nu=NU, nsteps=W)
+    torch.cuda.synchronize(dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident throughput (the graph-launched step)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        barrier()
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        plan.step(state, dt=DT, nu=NU, nsteps=K)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        barrier()
+    launches = plan.last_launch_count
+    ms = e0.elapsed_time(e1)
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * K / (ms_max / 1e3)
+
+    # ---- end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        series_host = torch.empty((1 + K // SAVE_EVERY + (1 if K % SAVE_EVERY else 0), 1, 8),
+                                  dtype=torch.float64).pin_memory()
+        final_host = torch.empty_like(init_host).pin_memory()
+        barrier()
+        torch.cuda.synchronize(dev)
+        e2 = torch.cuda.Event(enable_timing=True)
+        e3 = torch.cuda.Event(enable_timing=True)
+        e2.record(stream)
+        state.copy_(init_host, non_blocking=True)
+        series = plan.run(state, dt=DT, nu=NU, nsteps=K, save_every=SAVE_EVERY)
+        series_host.copy_(series, non_blocking=True)
+        final_host.copy_(state, non_blocking=True)
+        e3.record(stream)
+        torch.cuda.synchronize(dev)
+        barrier()
+        e2e_launches = plan.last_launch_count
+        t2 = torch.tensor([e2.elapsed_time(e3)], dtype=torch.float64, device=dev)
+        if world > 1:
+            torch.distributed.all_reduce(t2, op=torch.distributed.ReduceOp.MAX)
+        sbytes = init_host.numel() * init_host.element_size()
+        e2e = {"value": world * K / (float(t2.item()) / 1e3), "unit": UNIT,
+               "h2d_bytes_per_step": sbytes / K,
+               "d2h_bytes_per_step": (sbytes + series_host.numel() * 8) / K,
+               "path": "Plan.run (tg_run via ctypes): initial state H2D from pinned host memory, "
+                       f"{K} steps with diagnostics every {SAVE_EVERY}, series and final state D2H",
+               "gpu_launches": e2e_launches,
+               "final_energy": float(series_host[-1, 0, 0])}
+
+    # ---- per-pass CUDA-event profile (eager launches on the same stream)
+    prof = plan.profile_passes(state, dt=DT, nu=NU, nsteps=3)
+    abytes = algorithmic_bytes(n)
+    peak, peak_kind = measured_peaks()
+    total_ms = sum(m * c for m, c in prof.values())
+    passes = {}
+    for k, (m, c) in prof.items():
+        b = abytes.get(k)
+        passes[k] = {"ms": m, "launches": c, "share": m * c / total_ms,
+                     "alg_bytes": b, "gbs": (b / (m * 1e-3) / 1e9) if b else None}
+    dom = max((k for k in passes if passes[k]["alg_bytes"]), key=lambda k: passes[k]["share"])
+    ach = passes[dom]["gbs"]
+    traffic = ncu_traffic(dom)
+    roofline = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "traffic": traffic, "kernel": dom, "peak_source": f"{peak_kind} hbm_gbs",
+                "alg_bytes_per_launch": abytes[dom]}
+    step_alg = step_bytes(n)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        times = cpu_step_seconds(n, budget=args.cpu_budget)
+        cores = os.cpu_count() or 1
+        cpu = {"value": len(times) / sum(times), "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{len(times)} RK4 step(s) of the {n}^3 TG workload by the reference JAX "
+                         "algorithm restated in NumPy/SciPy FP64, FFTs threaded over all cores"}
+
+    clocks = clk.summary()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"taylor_green_hydro_{n}^3_fp32", "n": n, "nu": NU, "dt": DT,
+                       "ic": "Taylor-Green", "l2": "inputs larger than L2 (no flush)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "grid_point_updates_per_s": value * n ** 3,
+            "hbm_step_bytes_model": step_alg,
+            "step_gbs": step_alg / (ms_max / K * 1e-3) / 1e9,
+            "step_frac_of_peak": step_alg / (ms_max / K * 1e-3) / 1e9 / peak,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clocks, "passes": passes,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    try:
+        run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

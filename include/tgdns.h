@@ -173,6 +173,16 @@ int tg_from_full_spectrum(tg_plan* plan, const void* full, void* state);
  * (cuda/taylor_green_mhd.py:62-69) evaluated on the grid values as given. */
 int tg_physical_energy(tg_plan* plan, const void* phys, double* out);
 
+/* Per-pass timing: runs nsteps RK4 steps eagerly (no graph) with a CUDA event
+ * pair around every kernel launch on the plan's stream, then writes, per pass
+ * kind (slot = internal pass op: 0/1 x-stage hydro/MHD, 2/3 x-load, 4/5 x-forward,
+ * 6 y-inverse, 7 y-forward, 8/9 z-product hydro/MHD, 10 z-C2R, 11 z-R2C), the mean
+ * launch duration in ms and the launch count.  The reference has no profiler; its
+ * only timing is wall-clock around the loop (jax/taylor_green_jax.py:264,277). */
+#define TG_PROF_SLOTS 12
+int tg_profile_passes(tg_plan* plan, void* state, double dt, double nu, double eta, int nsteps,
+                      double ms[TG_PROF_SLOTS], int64_t count[TG_PROF_SLOTS]);
+
 /* Kernels launched by the last tg_step / tg_run call (for launch accounting). */
 int64_t tg_last_launch_count(const tg_plan* plan);
 

@@ -22,6 +22,10 @@ TG_IC_TAYLOR_GREEN, TG_IC_MHD_REFERENCE, TG_IC_MHD_EQUAL_ENERGY, TG_IC_ZERO = ra
 TG_ABSMAX_VELOCITY, TG_ABSMAX_DIVERGENCE = 0, 1
 TG_DERIVED_VORTICITY, TG_DERIVED_DIVERGENCE = 0, 1
 TG_DIAG_WIDTH = 8
+TG_PROF_SLOTS = 12
+PASS_NAMES = ("kx_stage_hd", "kx_stage_mhd", "kx_load_hd", "kx_load_mhd", "kx_fwd_hd",
+              "kx_fwd_mhd", "ky_inverse", "ky_forward", "kz_product_hd", "kz_product_mhd",
+              "kz_c2r", "kz_r2c")
 (TG_D_KINETIC, TG_D_ENSTROPHY, TG_D_DISSIPATION, TG_D_MAGNETIC, TG_D_CROSS_HELICITY,
  TG_D_TOTAL, TG_D_DIVU_MAX, TG_D_DIVB_MAX) = range(8)
 
@@ -52,6 +56,8 @@ SIGNATURES = {
     "tg_to_full_spectrum": (c_int, [c_void_p, c_void_p, c_void_p]),
     "tg_from_full_spectrum": (c_int, [c_void_p, c_void_p, c_void_p]),
     "tg_physical_energy": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "tg_profile_passes": (c_int, [c_void_p, c_void_p, c_double, c_double, c_double, c_int,
+                                  ctypes.POINTER(c_double), ctypes.POINTER(c_int64)]),
     "tg_last_launch_count": (c_int64, [c_void_p]),
     "tg_last_error": (ctypes.c_char_p, []),
     "tg_version": (c_int, []),

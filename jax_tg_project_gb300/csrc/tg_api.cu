@@ -362,10 +362,16 @@ static int cuda_fail(cudaError_t e, const char* where) {
     if (e_ != cudaSuccess) return cuda_fail(e_, where); \
   } while (0)
 
+struct ProfEvent {
+  int op;
+  cudaEvent_t start, stop;
+};
+
 struct tg_plan {
   Geo g{};
   int n = 0, K = 0, batch = 1, F = 3, G = 6, physics = 0, prec = 0, flags = 0;
   cudaStream_t st = nullptr;
+  cudaStream_t cap = nullptr;  // private non-blocking stream used only to capture the step graph
   void* X = nullptr;    // [batch][G][N][M][Hz]
   void* Y = nullptr;    // [batch][G][N][N][Hz]; W aliases it
   void* Z = nullptr;    // [batch][F][N][N][Hz]
@@ -384,6 +390,8 @@ struct tg_plan {
   const void* step_state = nullptr;
   int64_t launches = 0;
   int64_t scratch = 0;
+  // per-launch CUDA events (op, start, stop) while tg_profile_passes runs
+  std::vector<ProfEvent>* prof = nullptr;
 };
 
 namespace {
@@ -409,8 +417,18 @@ struct Ops {
     return a;
   }
   static int go(tg_plan* p, int op, const PassArgs<R>& a, const char* what) {
+    ProfEvent pe{op, nullptr, nullptr};
+    if (p->prof) {
+      TG_CUDA(cudaEventCreate(&pe.start), "event");
+      TG_CUDA(cudaEventCreate(&pe.stop), "event");
+      TG_CUDA(cudaEventRecord(pe.start, p->st), "event record");
+    }
     cudaError_t e = launcher<R>(p)(op, a, p->batch, p->st);
     ++p->launches;
+    if (p->prof) {
+      cudaEventRecord(pe.stop, p->st);
+      p->prof->push_back(pe);
+    }
     if (e != cudaSuccess) return cuda_fail(e, what);
     return TG_OK;
   }
@@ -638,12 +656,18 @@ int advance(tg_plan* p, void* S, int nsteps) {
     rc = dispatch(p, [&](auto ops) { return decltype(ops)::stages(p, S); });
     if (rc) return rc;
     done = 1;
-    TG_CUDA(cudaStreamBeginCapture(p->st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    // capture on the plan's private stream (the caller's may be the legacy default
+    // stream, which cannot be captured); the graph is then launched on the caller's
+    if (!p->cap) TG_CUDA(cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking), "capture stream");
+    cudaStream_t user = p->st;
+    TG_CUDA(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal), "begin capture");
     const int64_t before = p->launches;
+    p->st = p->cap;
     rc = dispatch(p, [&](auto ops) { return decltype(ops)::stages(p, S); });
+    p->st = user;
     p->launches = before;
     cudaGraph_t graph = nullptr;
-    cudaError_t e = cudaStreamEndCapture(p->st, &graph);
+    cudaError_t e = cudaStreamEndCapture(p->cap, &graph);
     if (rc) {
       if (graph) cudaGraphDestroy(graph);
       return rc;
@@ -775,6 +799,7 @@ int tg_plan_create(tg_plan** out, const tg_desc* d) {
 int tg_plan_destroy(tg_plan* p) {
   if (!p) return TG_OK;
   drop_graph(p);
+  if (p->cap) cudaStreamDestroy(p->cap);
   void* bufs[] = {p->X, p->Y, p->Z, p->ACC, p->VS, p->TW, p->part, p->dtmp, p->amax, p->coef};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -967,6 +992,44 @@ int tg_physical_energy(tg_plan* p, const void* phys, double* out) {
   if (!p || !phys || !out) return fail(TG_E_INVALID, "tg_physical_energy: null argument");
   p->launches = 0;
   return dispatch(p, [&](auto ops) { return decltype(ops)::energy(p, phys, out); });
+}
+
+int tg_profile_passes(tg_plan* p, void* state, double dt, double nu, double eta, int nsteps, double* ms,
+                      int64_t* count) {
+  if (!p || !state || !ms || !count) return fail(TG_E_INVALID, "tg_profile_passes: null argument");
+  if (nsteps < 1) return fail(TG_E_INVALID, "tg_profile_passes: nsteps must be >= 1");
+  int rc = set_coefs(p, dt, nu, eta);
+  if (rc) return rc;
+  for (int i = 0; i < TG_PROF_SLOTS; ++i) {
+    ms[i] = 0.0;
+    count[i] = 0;
+  }
+  std::vector<ProfEvent> ev;
+  p->prof = &ev;
+  p->launches = 0;
+  rc = dispatch(p, [&](auto ops) {
+    using O = decltype(ops);
+    int r = O::start(p, state);
+    for (int s = 0; s < nsteps && !r; ++s) r = O::stages(p, state);
+    return r;
+  });
+  p->prof = nullptr;
+  cudaError_t e = cudaStreamSynchronize(p->st);
+  for (auto& pe : ev) {
+    float t = 0.f;
+    if (!rc && e == cudaSuccess && cudaEventElapsedTime(&t, pe.start, pe.stop) == cudaSuccess &&
+        pe.op >= 0 && pe.op < TG_PROF_SLOTS) {
+      ms[pe.op] += t;
+      count[pe.op] += 1;
+    }
+    cudaEventDestroy(pe.start);
+    cudaEventDestroy(pe.stop);
+  }
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "tg_profile_passes");
+  for (int i = 0; i < TG_PROF_SLOTS; ++i)
+    if (count[i]) ms[i] /= (double)count[i];
+  return TG_OK;
 }
 
 }  // extern "C"

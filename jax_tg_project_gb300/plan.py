@@ -177,6 +177,55 @@ class Plan:
         check(self.lib.tg_diagnostics(self._h, _ptr(state), float(nu), float(eta), _ptr(out)))
         return out
 
+    def profile_passes(self, state, dt=-1.0, nu=-1.0, eta=-1.0, nsteps=1):
+        """Mean CUDA-event duration (ms) and count of each pass kind over nsteps eager steps."""
+        self._check_state(state)
+        ms = (ctypes.c_double * _abi.TG_PROF_SLOTS)()
+        cnt = (ctypes.c_int64 * _abi.TG_PROF_SLOTS)()
+        self._sync_stream()
+        check(self.lib.tg_profile_passes(self._h, _ptr(state), float(dt), float(nu), float(eta),
+                                         int(nsteps), ms, cnt))
+        return {name: (ms[i], int(cnt[i])) for i, name in enumerate(_abi.PASS_NAMES) if cnt[i]}
+
+    def derived(self, state, which="vorticity"):
+        """Physical curl (vorticity [, current]) or divergence field(s) of a state."""
+        self._check_state(state)
+        sel = _abi.TG_DERIVED_VORTICITY if which == "vorticity" else _abi.TG_DERIVED_DIVERGENCE
+        nf = self.F if sel == _abi.TG_DERIVED_VORTICITY else self.F // 3
+        out = torch.empty((self.batch, nf, self.n, self.n, self.n), dtype=self.real_dtype,
+                          device=self.device)
+        self._sync_stream()
+        check(self.lib.tg_derived(self._h, _ptr(state), sel, _ptr(out)))
+        return out
+
+    def to_full(self, state):
+        """State -> full complex fftn layout (batch, F, n, n, n), unnormalised."""
+        self._check_state(state)
+        out = torch.empty((self.batch, self.F, self.n, self.n, self.n), dtype=self.complex_dtype,
+                          device=self.device)
+        self._sync_stream()
+        check(self.lib.tg_to_full_spectrum(self._h, _ptr(state), _ptr(out)))
+        return out
+
+    def from_full(self, full, out=None):
+        shape = (self.batch, self.F, self.n, self.n, self.n)
+        if not (isinstance(full, torch.Tensor) and full.is_cuda and full.dtype == self.complex_dtype
+                and tuple(full.shape) == shape and full.is_contiguous()):
+            raise ValueError(f"full spectrum must be a contiguous {self.complex_dtype} CUDA tensor "
+                             f"of shape {shape}")
+        s = self._check_state(out) if out is not None else self.new_state()
+        self._sync_stream()
+        check(self.lib.tg_from_full_spectrum(self._h, _ptr(full), _ptr(s)))
+        return s
+
+    def physical_energy(self, phys):
+        """0.5 <|u|^2> [, 0.5 <|b|^2>] of physical fields, FP64, shape (batch, F/3)."""
+        self._check_phys(phys)
+        out = torch.zeros((self.batch, self.F // 3), dtype=torch.float64, device=self.device)
+        self._sync_stream()
+        check(self.lib.tg_physical_energy(self._h, _ptr(phys), _ptr(out)))
+        return out
+
     def absmax(self, state, which="velocity"):
         self._check_state(state)
         sel = _abi.TG_ABSMAX_VELOCITY if which == "velocity" else _abi.TG_ABSMAX_DIVERGENCE
