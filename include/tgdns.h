@@ -186,6 +186,27 @@ int tg_profile_passes(tg_plan* plan, void* state, double dt, double nu, double e
 /* Kernels launched by the last tg_step / tg_run call (for launch accounting). */
 int64_t tg_last_launch_count(const tg_plan* plan);
 
+/* Allocation-free diagnostics.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory when they need the energies (a
+ * framework that owns all device memory and forbids cudaMalloc inside its
+ * operators, a fixed-footprint real-time loop) and therefore cannot create a
+ * plan.  Computes records 0-5 of tg_diagnostics (E_k, enstrophy, nu*sum k^2|u|^2,
+ * E_m, H_c, E_k+E_m) of a state laid out as a plan with the default 2/3 cutoff
+ * would lay it out (n, batch, physics, precision as in tg_desc) into out
+ * ([batch][TG_DIAG_WIDTH] doubles, device); slots 6-7 (divergence maxima) are
+ * not computed and are set to -1.  Its only scratch is a file-scope device
+ * array of TG_NOALLOC_MAX_RUNS*96*5 doubles (240 KiB) that every GPU loading the
+ * library holds until the process exits; batch > TG_NOALLOC_MAX_RUNS is rejected
+ * with TG_E_INVALID.  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current: make that first call
+ * before any stream capture.  All calls share the array: calls that overlap on
+ * the GPU race and must be ordered by the caller.  Calls no cudaMalloc/cudaFree
+ * and no allocating library routine.  eta is unused (kept for symmetry with
+ * tg_diagnostics).  Asynchronous on stream. */
+#define TG_NOALLOC_MAX_RUNS 64
+int tg_diagnostics_noalloc(const void* state, int n, int batch, int physics, int precision, double nu,
+                           double eta, double* out, void* stream);
+
 const char* tg_last_error(void);
 int tg_version(void);
 

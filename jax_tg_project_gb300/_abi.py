@@ -23,6 +23,7 @@ TG_ABSMAX_VELOCITY, TG_ABSMAX_DIVERGENCE = 0, 1
 TG_DERIVED_VORTICITY, TG_DERIVED_DIVERGENCE = 0, 1
 TG_DIAG_WIDTH = 8
 TG_PROF_SLOTS = 12
+TG_NOALLOC_MAX_RUNS = 64
 PASS_NAMES = ("kx_stage_hd", "kx_stage_mhd", "kx_load_hd", "kx_load_mhd", "kx_fwd_hd",
               "kx_fwd_mhd", "ky_inverse", "ky_forward", "kz_product_hd", "kz_product_mhd",
               "kz_c2r", "kz_r2c")
@@ -58,6 +59,8 @@ SIGNATURES = {
     "tg_physical_energy": (c_int, [c_void_p, c_void_p, c_void_p]),
     "tg_profile_passes": (c_int, [c_void_p, c_void_p, c_double, c_double, c_double, c_int,
                                   ctypes.POINTER(c_double), ctypes.POINTER(c_int64)]),
+    "tg_diagnostics_noalloc": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_double, c_double,
+                                       c_void_p, c_void_p]),
     "tg_last_launch_count": (c_int64, [c_void_p]),
     "tg_last_error": (ctypes.c_char_p, []),
     "tg_version": (c_int, []),

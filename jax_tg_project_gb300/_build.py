@@ -65,7 +65,8 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
             if f.read().strip() == digest:
                 return LIB
     nvcc = _nvcc()
-    units = [(os.path.join(CSRC, "tg_api.cu"), os.path.join(BUILD, "tg_api.o"), [])]
+    units = [(os.path.join(CSRC, "tg_api.cu"), os.path.join(BUILD, "tg_api.o"), []),
+             (os.path.join(CSRC, "tg_noalloc.cu"), os.path.join(BUILD, "tg_noalloc.o"), [])]
     for real, sizes in (("float", SIZES_F32), ("double", SIZES_F64)):
         for n in sizes:
             units.append((os.path.join(CSRC, "tg_inst.cu"),

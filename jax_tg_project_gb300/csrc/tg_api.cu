@@ -349,6 +349,11 @@ using namespace tg;
 
 static thread_local std::string g_last_error;
 
+namespace tg {
+// lets other translation units of the library report through tg_last_error()
+void set_last_error(const std::string& message) { g_last_error = message; }
+}  // namespace tg
+
 static int fail(int code, const std::string& msg) {
   g_last_error = msg;
   return code;

@@ -1,0 +1,178 @@
+// Allocation-free spectral diagnostics: tg_diagnostics_noalloc (include/tgdns.h).
+//
+// Why: some callers cannot allocate device memory at the point where they want
+// the energies -- a host framework that owns every device buffer and forbids
+// cudaMalloc inside its custom-call / operator execution (an XLA FFI handler, a
+// PyTorch operator under a caching allocator it must not bypass), or a real-time
+// loop that runs with a fixed memory footprint.  tg_diagnostics needs a plan,
+// and creating a plan allocates.  This entry point needs no plan: the only
+// scratch is the block partial sums, held in the file-scope device array below.
+//
+// The array is part of the library image: every GPU that loads the library
+// holds it (TG_NOALLOC_MAX_RUNS * 96 * 5 doubles = 240 KiB) until the process
+// exits.  All calls share it and it keeps the previous call's contents; each
+// call overwrites every slot it reads, so nothing needs clearing.  Calls that
+// overlap on the GPU (different streams, or host threads racing on one device)
+// race on the array and must be ordered by the caller.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <mutex>
+#include <string>
+
+#include "../../include/tgdns.h"
+#include "tg_common.cuh"
+
+namespace tg {
+void set_last_error(const std::string& message);  // tg_api.cu
+}
+
+namespace {
+
+constexpr int kBlocks = 96;   // partial sums per run
+constexpr int kThreads = 256;
+constexpr int kQ = 5;         // E_k, enstrophy, sum w k^2 |u|^2, E_m, H_c
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) double g_partials[TG_NOALLOC_MAX_RUNS * kBlocks * kQ];
+
+// host copy of the array's device address, looked up once per device
+std::mutex g_mu;
+double* g_addr[kMaxDevices] = {nullptr};
+
+
+struct Comp {
+  double s = 0.0, c = 0.0;
+  __device__ void add(double x) {
+    const double t = s + x;
+    c += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
+    s = t;
+  }
+  __device__ double value() const { return s + c; }
+};
+
+template <typename R>
+__global__ void __launch_bounds__(kThreads) partial_kernel(const tg::cplx<R>* S, tg::Geo g, int F, double* part) {
+  using C = tg::cplx<R>;
+  const int run = blockIdx.y;
+  const C* base = S + (long long)run * F * g.sS;
+  const long long total = (long long)g.M * g.M * g.Hk;
+  Comp q[kQ];
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int kz = int(idx % g.Hk);
+    const long long r = idx / g.Hk;
+    const int iy = int(r % g.M), ix = int(r / g.M);
+    const double kx = tg::ksigned(ix, g.K), ky = tg::ksigned(iy, g.K), kzd = kz;
+    const double w = (kz == 0) ? 1.0 : 2.0;
+    const long long o = ((long long)ix * g.M + iy) * g.Hz + kz;
+    const C ux = base[o], uy = base[g.sS + o], uz = base[2 * g.sS + o];
+    const double e2 = double(ux.x) * ux.x + double(ux.y) * ux.y + double(uy.x) * uy.x +
+                      double(uy.y) * uy.y + double(uz.x) * uz.x + double(uz.y) * uz.y;
+    const double cxr = ky * uz.x - kzd * uy.x, cxi = ky * uz.y - kzd * uy.y;
+    const double cyr = kzd * ux.x - kx * uz.x, cyi = kzd * ux.y - kx * uz.y;
+    const double czr = kx * uy.x - ky * ux.x, czi = kx * uy.y - ky * ux.y;
+    q[0].add(0.5 * w * e2);
+    q[1].add(0.5 * w * (cxr * cxr + cxi * cxi + cyr * cyr + cyi * cyi + czr * czr + czi * czi));
+    q[2].add(w * (kx * kx + ky * ky + kzd * kzd) * e2);
+    if (F == 6) {
+      const C bx = base[3 * g.sS + o], by = base[4 * g.sS + o], bz = base[5 * g.sS + o];
+      q[3].add(0.5 * w * (double(bx.x) * bx.x + double(bx.y) * bx.y + double(by.x) * by.x +
+                          double(by.y) * by.y + double(bz.x) * bz.x + double(bz.y) * bz.y));
+      q[4].add(w * (double(ux.x) * bx.x + double(ux.y) * bx.y + double(uy.x) * by.x +
+                    double(uy.y) * by.y + double(uz.x) * bz.x + double(uz.y) * bz.y));
+    }
+  }
+  __shared__ double sh[kQ][kThreads];
+  for (int i = 0; i < kQ; ++i) sh[i][threadIdx.x] = q[i].value();
+  __syncthreads();
+  for (int s = kThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int i = 0; i < kQ; ++i) sh[i][threadIdx.x] += sh[i][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x < kQ) part[((long long)run * kBlocks + blockIdx.x) * kQ + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void final_kernel(const double* part, double nu, int F, double* out) {
+  const int run = blockIdx.x;
+  __shared__ double v[kQ];
+  if (threadIdx.x < kQ) {
+    Comp s;
+    for (int b = 0; b < kBlocks; ++b) s.add(part[((long long)run * kBlocks + b) * kQ + threadIdx.x]);
+    v[threadIdx.x] = s.value();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double* o = out + (long long)run * TG_DIAG_WIDTH;
+    o[TG_D_KINETIC] = v[0];
+    o[TG_D_ENSTROPHY] = v[1];
+    o[TG_D_DISSIPATION] = nu * v[2];
+    o[TG_D_MAGNETIC] = (F == 6) ? v[3] : 0.0;
+    o[TG_D_CROSS_HELICITY] = (F == 6) ? v[4] : 0.0;
+    o[TG_D_TOTAL] = v[0] + ((F == 6) ? v[3] : 0.0);
+    o[TG_D_DIVU_MAX] = -1.0;  // not computed here (needs transform scratch)
+    o[TG_D_DIVB_MAX] = -1.0;
+  }
+}
+
+int fail(int code, const std::string& m) {
+  tg::set_last_error(m);  // reported by tg_last_error()
+  return code;
+}
+
+// the device address of g_partials for the current device (looked up once)
+int partials_address(double** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(TG_E_CUDA, std::string("tg_diagnostics_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices) return fail(TG_E_UNSUPPORTED, "tg_diagnostics_noalloc: device index too large");
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (!g_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_partials);
+    if (e != cudaSuccess || !p)
+      return fail(TG_E_CUDA, std::string("tg_diagnostics_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    g_addr[dev] = static_cast<double*>(p);
+  }
+  *out = g_addr[dev];
+  return TG_OK;
+}
+
+}  // namespace
+
+extern "C" int tg_diagnostics_noalloc(const void* state, int n, int batch, int physics, int precision, double nu,
+                                      double eta, double* out, void* stream) {
+  (void)eta;
+  if (!state || !out) return fail(TG_E_INVALID, "tg_diagnostics_noalloc: null argument");
+  if (n < 4) return fail(TG_E_INVALID, "tg_diagnostics_noalloc: n must be at least 4");
+  if (physics != TG_PHYS_HYDRO && physics != TG_PHYS_MHD)
+    return fail(TG_E_INVALID, "tg_diagnostics_noalloc: physics must be TG_PHYS_HYDRO or TG_PHYS_MHD");
+  if (precision != TG_PREC_F32 && precision != TG_PREC_F64)
+    return fail(TG_E_INVALID, "tg_diagnostics_noalloc: precision must be TG_PREC_F32 or TG_PREC_F64");
+  if (batch < 1 || batch > TG_NOALLOC_MAX_RUNS)
+    return fail(TG_E_INVALID, "tg_diagnostics_noalloc: batch " + std::to_string(batch) +
+                                  " is outside 1.." + std::to_string(TG_NOALLOC_MAX_RUNS) +
+                                  " (the fixed size of its static scratch)");
+  double* part = nullptr;
+  int rc = partials_address(&part);
+  if (rc) return rc;
+  tg::Geo g{};
+  g.n = n;
+  g.K = n / 3;
+  g.M = 2 * g.K + 1;
+  g.Hk = g.K + 1;
+  g.Hz = (g.Hk + 3) / 4 * 4;
+  g.sS = (long long)g.M * g.M * g.Hz;
+  const int F = physics == TG_PHYS_MHD ? 6 : 3;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  dim3 grid(kBlocks, batch);
+  if (precision == TG_PREC_F64)
+    partial_kernel<double><<<grid, kThreads, 0, st>>>(static_cast<const tg::cplx<double>*>(state), g, F, part);
+  else
+    partial_kernel<float><<<grid, kThreads, 0, st>>>(static_cast<const tg::cplx<float>*>(state), g, F, part);
+  final_kernel<<<batch, 32, 0, st>>>(part, nu, F, out);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(TG_E_CUDA, std::string("tg_diagnostics_noalloc: launch: ") + cudaGetErrorString(e));
+  return TG_OK;
+}
