@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -395,6 +396,7 @@ struct tg_plan {
   const void* step_state = nullptr;
   int64_t launches = 0;
   int64_t scratch = 0;
+  int variant = 0;  // pass-kernel variant (TG_PASS_VARIANT=1 selects the shared-memory passes)
   // per-launch CUDA events (op, start, stop) while tg_profile_passes runs
   std::vector<ProfEvent>* prof = nullptr;
 };
@@ -418,6 +420,7 @@ struct Ops {
     a.tw = static_cast<const C*>(p->TW);
     a.coef = p->coef;
     a.amax = p->amax;
+    a.variant = p->variant;
     if (p->flags & TG_FLAG_EXPLICIT_VISC) a.flags |= FLAG_EXPLICIT;
     return a;
   }
@@ -730,6 +733,7 @@ int tg_plan_create(tg_plan** out, const tg_desc* d) {
   p->flags = d->flags;
   p->F = d->physics == TG_PHYS_MHD ? 6 : 3;
   p->G = 2 * p->F;
+  if (const char* v = std::getenv("TG_PASS_VARIANT")) p->variant = std::atoi(v);
   Geo& g = p->g;
   g.n = n;
   g.K = K;

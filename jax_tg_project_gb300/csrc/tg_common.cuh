@@ -92,6 +92,7 @@ template <typename R> struct PassArgs {
   int flags;
   int map;               // FieldMap for KX_LOAD
   int nin, nout;         // fields read / written by this pass
+  int variant;           // 0: register-resident x/z passes where built, 1: shared-memory passes
 };
 
 // signed wavenumber of compact index i (0..M-1)

@@ -9,8 +9,8 @@
 // writes y[(j/Ns)*Ns*R + (j mod Ns) + r*Ns].  The first pass reads through a
 // caller functor (global memory, Hermitian packing, a spectral formula ...),
 // the last pass hands each result to a caller functor; intermediate data sit
-// in a padded shared-memory column.  Twiddles W_N^m come from a table
-// generated in FP64 on the host.
+// in a padded shared-memory column.  Twiddles come from a table generated in
+// FP64 on the host, rearranged per pass in shared memory (build_twiddles).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -129,22 +129,61 @@ struct FftPlan {
   static constexpr int E = N_ / P_;  // elements held per thread per pass
 };
 
-// padded shared-memory index: one spare slot every 16 complex values
-__device__ __forceinline__ int padx(int n) { return n + (n >> 4); }
-template <int N> struct ColLayout {
-  // per-column stride in complex elements (odd, so that columns interleave banks)
-  static constexpr int PADN = N + (N >> 4);
-  static constexpr int CS = (PADN % 2 == 0) ? PADN + 1 : PADN;
+// padded shared-memory index: one spare slot every 2^PSH complex values
+template <int PSH = 4>
+__device__ __forceinline__ int padx(int n) { return n + (n >> PSH); }
+// per-column stride in complex elements, congruent to CSMOD modulo 16 (the 16
+// eight-byte bank pairs), so that the columns of a CTA interleave banks
+template <int N, int PSH = 4, int CSMOD = 1> struct ColLayout {
+  static constexpr int PADN = N + (N >> PSH);
+  static constexpr int CS = PADN + (((CSMOD - PADN) % 16) + 16) % 16;
+};
+
+// Per-pass twiddle tables: pass I (sub-length NS, radix R) uses W_{NS R}^{jm r}
+// for jm < NS, 1 <= r < R, stored at offset (NS - R0) + (r - 1) NS + jm, so the
+// threads of a warp (consecutive jm) read consecutive slots.  The blocks add up
+// to N - R0 < N entries.  Values are copied from the FP64-generated W_N table.
+template <class Plan, int I = 0, int NS = 1, typename C>
+__device__ __forceinline__ void build_twiddles(C* dst, const C* wn, int tid, int nthr) {
+  if constexpr (I < Plan::NPASS) {
+    constexpr int R = Plan::template radix<I>();
+    if constexpr (I > 0) {
+      constexpr int OFF = NS - Plan::template radix<0>();
+      for (int e = tid; e < (R - 1) * NS; e += nthr) {
+        const int r = 1 + e / NS, jm = e % NS;
+        dst[OFF + e] = wn[jm * r * (Plan::N / (NS * R))];
+      }
+    }
+    build_twiddles<Plan, I + 1, NS * R>(dst, wn, tid, nthr);
+  }
+}
+
+// Barriers between passes: the threads that share exchange columns.
+struct CtaSync {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+struct WarpSync {
+  __device__ __forceinline__ void operator()() const { __syncwarp(); }
+};
+struct NamedSync {  // bar.sync on a named barrier shared by `count` threads (whole warps)
+  int id, count;
+  __device__ __forceinline__ void operator()() const {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+  }
 };
 
 // Execute pass I of Plan for one column.
-//   src(n)            -> value at input index n (pass 0 only)
+//   src(n, q)         -> value at input index n (pass 0 only); q = (n - t) / P
 //   dst(b, r, k, v)   <- output v at index k (last pass); b, r compile-time
 //   xb                -> this column's padded shared-memory buffer
-//   tw                -> table W_N^m (forward sign), shared or global
-// All threads of the CTA must call this together (it contains __syncthreads).
-template <class Plan, int DIR, int I, int NS, typename C, class Src, class Dst>
-__device__ __forceinline__ void fft_pass(int t, Src& src, Dst& dst, C* xb, const C* tw) {
+//   tw                -> per-pass twiddle tables (build_twiddles), forward sign
+//   sync()            -> barrier over every thread using the exchange columns
+// Thread t reads exactly the inputs n = t (mod P) in pass 0 and holds exactly the
+// outputs k = t (mod P) after the last pass (q = b + r*N/(R*P) in both), so a
+// transform can take its input from, and leave its output in, registers.
+template <class Plan, int DIR, int I, int NS, int PSH = 4, typename C, class Src, class Dst, class Sync = CtaSync>
+__device__ __forceinline__ void fft_pass(int t, Src& src, Dst& dst, C* xb, const C* tw,
+                                         const Sync& sync = Sync()) {
   constexpr int N = Plan::N, P = Plan::P;
   constexpr int R = Plan::template radix<I>();
   constexpr int NB = N / (R * P);
@@ -156,16 +195,16 @@ __device__ __forceinline__ void fft_pass(int t, Src& src, Dst& dst, C* xb, const
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       if constexpr (I == 0) {
-        v[b][r] = src(j + r * (N / R));
+        v[b][r] = src(j + r * (N / R), b + r * NB);
       } else {
-        v[b][r] = xb[padx(j + r * (N / R))];
+        v[b][r] = xb[padx<PSH>(j + r * (N / R))];
       }
     }
     if constexpr (I > 0) {
       const int jm = j % NS;
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        C w = tw[jm * r * (N / (NS * R))];
+        C w = tw[(NS - Plan::template radix<0>()) + (r - 1) * NS + jm];
         if constexpr (DIR > 0) w.y = -w.y;
         v[b][r] = cmul(v[b][r], w);
       }
@@ -173,17 +212,17 @@ __device__ __forceinline__ void fft_pass(int t, Src& src, Dst& dst, C* xb, const
     dft<R, DIR>(v[b]);
   }
   if constexpr (!LAST) {
-    __syncthreads();  // every reader of xb (this or a previous transform) is done
+    sync();  // every reader of xb (this or a previous transform) is done
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
       const int j = t + P * b;
       const int jm = j % NS;
       const int base = (j / NS) * NS * R + jm;
 #pragma unroll
-      for (int r = 0; r < R; ++r) xb[padx(base + r * NS)] = v[b][r];
+      for (int r = 0; r < R; ++r) xb[padx<PSH>(base + r * NS)] = v[b][r];
     }
-    __syncthreads();
-    fft_pass<Plan, DIR, I + 1, NS * R>(t, src, dst, xb, tw);
+    sync();
+    fft_pass<Plan, DIR, I + 1, NS * R, PSH>(t, src, dst, xb, tw, sync);
   } else {
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
@@ -194,9 +233,16 @@ __device__ __forceinline__ void fft_pass(int t, Src& src, Dst& dst, C* xb, const
   }
 }
 
-template <class Plan, int DIR, typename C, class Src, class Dst>
-__device__ __forceinline__ void fft_column(int t, Src& src, Dst& dst, C* xb, const C* tw) {
-  fft_pass<Plan, DIR, 0, 1>(t, src, dst, xb, tw);
+template <class Plan, int DIR, int PSH = 4, typename C, class Src, class Dst, class Sync = CtaSync>
+__device__ __forceinline__ void fft_column(int t, Src& src, Dst& dst, C* xb, const C* tw,
+                                           const Sync& sync = Sync()) {
+  fft_pass<Plan, DIR, 0, 1, PSH>(t, src, dst, xb, tw, sync);
+}
+
+// register slot q of the output (b, r) of the last pass
+template <class Plan>
+__host__ __device__ constexpr int out_slot(int b, int r) {
+  return b + r * (Plan::N / (Plan::template radix<Plan::NPASS - 1>() * Plan::P));
 }
 
 // index of output element (b, r) held by thread t after the last pass

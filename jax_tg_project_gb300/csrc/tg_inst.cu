@@ -1,7 +1,9 @@
 // One (real type, grid size) instantiation of the pass kernels.  The build
 // compiles this file once per supported pair with -DTG_REAL=float|double and
 // -DTG_N=<n>, so the translation units compile in parallel.
-#include "tg_kernels.cuh"
+#include <type_traits>
+
+#include "tg_kernels_reg.cuh"
 
 #ifndef TG_REAL
 #error "define TG_REAL (float or double)"
@@ -15,6 +17,14 @@
 
 namespace tg {
 cudaError_t TG_CAT(launch, TG_REAL, TG_N)(int op, const PassArgs<TG_REAL>& a, int runs, cudaStream_t st) {
+  if constexpr (std::is_same<TG_REAL, float>::value && HasRegPlan<TG_N>::value) {
+    if (a.variant == 0) {
+      if (op == OP_KZ_PROD_HD) return launch_kz_reg<TG_REAL, TG_N>(a, runs, st);
+      if (op == OP_KX_STAGE3) return launch_kx_reg<TG_REAL, TG_N, KX_STAGE>(a, runs, st);
+      if (op == OP_KX_LOAD3 && a.map == MAP_UW && a.nin == 3 && a.nout == 6)
+        return launch_kx_reg<TG_REAL, TG_N, KX_LOAD>(a, runs, st);
+    }
+  }
   return launch_pass<TG_REAL, TG_N>(op, a, runs, st);
 }
 }  // namespace tg

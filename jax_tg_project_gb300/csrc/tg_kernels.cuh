@@ -130,7 +130,7 @@ kx_kernel(const PassArgs<R> a) {
   const int kz = z0 + col;
   const bool zok = kz < g.Hk;
   C* xcol = xb + col * CS;
-  for (int i = threadIdx.x; i < N; i += NT) tw[i] = a.tw[i];
+  build_twiddles<Plan>(tw, a.tw, threadIdx.x, NT);
   const float kyf = float(ksigned(iyc, K)), kzf = float(kz);
 
   if constexpr (MODE == KX_LOAD) {
@@ -148,7 +148,7 @@ kx_kernel(const PassArgs<R> a) {
     const C* win = a.in + (long long)run * a.nin * g.sX + (long long)iyc * Hz + kz;
     for (int f = 0; f < a.nin; ++f) {
       const C* wf = win + f * g.sX;
-      auto src = [&](int x) -> C { return zok ? wf[(long long)x * M * Hz] : czero<C>(); };
+      auto src = [&](int x, int) -> C { return zok ? wf[(long long)x * M * Hz] : czero<C>(); };
       auto dst = [&](int, int, int k, C v) {
         const int ic = kcompact(k, N, K);
         if (ic >= 0) sb[(f * M + ic) * TZ + col] = cscale(v, inv_n3);
@@ -222,7 +222,7 @@ kx_kernel(const PassArgs<R> a) {
     const int map = (MODE == KX_STAGE) ? (F == 6 ? MAP_UWBJ : MAP_UW) : a.map;
     C* xo = a.out + (long long)run * a.nout * g.sX + (long long)iyc * Hz + kz;
     for (int gi = 0; gi < a.nout; ++gi) {
-      auto src = [&](int k) -> C {
+      auto src = [&](int k, int) -> C {
         const int ic = kcompact(k, N, K);
         if (!zok || ic < 0) return czero<C>();
         return field_value<C>(map, gi, sb, ic, col, M, TZ, float(ksigned(ic, K)), kyf, kzf);
@@ -253,13 +253,13 @@ ky_kernel(const PassArgs<R> a) {
   const int f = blockIdx.z % a.nin, run = blockIdx.z / a.nin;
   const int kz = z0 + col;
   const bool zok = kz < g.Hk;
-  for (int i = threadIdx.x; i < N; i += NT) tw[i] = a.tw[i];
+  build_twiddles<Plan>(tw, a.tw, threadIdx.x, NT);
   __syncthreads();
   C* xcol = xb + col * CS;
   if constexpr (DIR > 0) {
     const C* in = a.in + ((long long)run * a.nin + f) * g.sX + (long long)x * M * Hz + kz;
     C* out = a.out + ((long long)run * a.nin + f) * g.sY + (long long)x * N * Hz + kz;
-    auto src = [&](int k) -> C {
+    auto src = [&](int k, int) -> C {
       const int ic = kcompact(k, N, K);
       return (zok && ic >= 0) ? in[(long long)ic * Hz] : czero<C>();
     };
@@ -270,7 +270,7 @@ ky_kernel(const PassArgs<R> a) {
   } else {
     const C* in = a.in + ((long long)run * a.nin + f) * g.sY + (long long)x * N * Hz + kz;
     C* out = a.out + ((long long)run * a.nin + f) * g.sX + (long long)x * M * Hz + kz;
-    auto src = [&](int y) -> C { return zok ? in[(long long)y * Hz] : czero<C>(); };
+    auto src = [&](int y, int) -> C { return zok ? in[(long long)y * Hz] : czero<C>(); };
     auto dst = [&](int, int, int k, C v) {
       const int ic = kcompact(k, N, K);
       if (zok && ic >= 0) out[(long long)ic * Hz] = v;
@@ -312,12 +312,12 @@ kz_kernel(const PassArgs<R> a) {
   const int pair = blockIdx.x * LP + lp, run = blockIdx.y;
   const int x = pair / (N / 2), y0 = 2 * (pair % (N / 2));
   const long long row0 = ((long long)x * N + y0) * Hz;  // row (x, y0); row (x, y0+1) is + Hz
-  for (int i = threadIdx.x; i < N; i += NT) tw[i] = a.tw[i];
+  build_twiddles<Plan>(tw, a.tw, threadIdx.x, NT);
   __syncthreads();
 
   // Hermitian packing of rows (x,y0) and (x,y0+1) of one spectral field: Z = A + iB
   auto packed = [&](const C* fld) {
-    return [=](int k) -> C {
+    return [=](int k, int) -> C {
       if (k <= K) {
         C A = fld[row0 + k], B = fld[row0 + Hz + k];
         if (k == 0) { A.y = 0; B.y = 0; }
@@ -430,7 +430,7 @@ kz_kernel(const PassArgs<R> a) {
     // forward transforms of the products
     for (int c = 0; c < F; ++c) {
       C* pc = ph + c * CS;
-      auto src = [&](int n) -> C { return pc[padx(n)]; };
+      auto src = [&](int n, int) -> C { return pc[padx(n)]; };
       fft_column<Plan, -1>(t, src, dst_reg, xcol, tw);
       __syncthreads();
 #pragma unroll
@@ -473,7 +473,7 @@ kz_kernel(const PassArgs<R> a) {
     auto dst_reg = [&](int b, int r, int, C v) { zr[b * RL + r] = v; };
     for (int f = 0; f < a.nin; ++f) {
       const R* pi = a.phys_in + ((long long)run * a.nin + f) * g.sP + ((long long)x * N + y0) * N;
-      auto src = [&](int n) -> C { return mk<C>(pi[n], pi[N + n]); };
+      auto src = [&](int n, int) -> C { return mk<C>(pi[n], pi[N + n]); };
       fft_column<Plan, -1>(t, src, dst_reg, xcol, tw);
       __syncthreads();
 #pragma unroll

@@ -1,0 +1,374 @@
+// Register-resident x and z passes of the hydro step (FP32, N = 8 ... 256).
+//
+// With P = N/8 threads per transform (E = 8 values each), thread t of a column
+// reads the inputs n = t (mod P) in the first pass and ends with the outputs
+// k = t (mod P) after the last pass (see fft_pass).  Everything that is
+// pointwise along the transformed axis therefore stays in the registers of the
+// thread that owns those indices:
+//
+//   kz_reg_kernel  one z line pair per P threads: six inverse transforms of the
+//                  Hermitian-packed rows (u, omega), u x omega in registers, three
+//                  forward transforms read straight from those registers, and the
+//                  Hermitian unpack Z(N-k) fetched from the partner lane by shuffle.
+//   kx_reg_kernel  four consecutive kz columns per group of 4P threads: the three
+//                  forward transforms, the fused 1/N^3 / Leray / RK4 stage and the
+//                  six inverse transforms all keep the column in registers.
+//
+// Shared memory holds only the twiddle table and one exchange column per
+// transform, so barriers are per warp (z) or per 4-column group (x, a named
+// barrier), never CTA-wide inside the loops.
+#pragma once
+
+#include <type_traits>
+
+#include "tg_kernels.cuh"
+
+namespace tg {
+
+template <int N> struct RegPlan;
+template <> struct RegPlan<8> { using T = FftPlan<8, 1, 8>; };
+template <> struct RegPlan<16> { using T = FftPlan<16, 2, 8, 2>; };
+template <> struct RegPlan<32> { using T = FftPlan<32, 4, 8, 4>; };
+template <> struct RegPlan<64> { using T = FftPlan<64, 8, 8, 8>; };
+template <> struct RegPlan<128> { using T = FftPlan<128, 16, 8, 2, 8>; };
+template <> struct RegPlan<256> { using T = FftPlan<256, 32, 8, 4, 8>; };
+
+// sizes with a register plan (N = 8 has fewer line pairs than one CTA holds)
+template <int N> struct HasRegPlan { static constexpr bool value = (N == 16 || N == 32 || N == 64 || N == 128 || N == 256); };
+
+// 16-byte asynchronous global -> shared copy (L1 bypass) and its completion wait
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory"); }
+
+// ------------------------------------------------------------------ z pass
+template <typename R, int N>
+struct KzRegShape {
+  using Plan = typename RegPlan<N>::T;
+  static constexpr int P = Plan::P, E = Plan::E;
+  static constexpr int NT = 128;
+  static constexpr int LP = NT / P;  // line pairs per CTA
+  static constexpr int PSH = (N >= 64) ? 4 : 3;  // exchange padding (bank-conflict model, see DESIGN)
+  static constexpr int CS = ColLayout<N, PSH, (N == 16) ? 2 : 4>::CS;
+  static constexpr int HZMAX = ((N / 3 + 1) + 3) / 4 * 4;
+  // per pair: exchange column + the two spectral rows of the six input fields
+  static constexpr long long per_pair = CS + 6LL * 2 * HZMAX;
+  static constexpr long long smem = (long long)sizeof(cplx<R>) * (N + (long long)LP * per_pair);
+};
+
+template <typename R, int N>
+__global__ void __launch_bounds__(128, 3) kz_reg_kernel(const PassArgs<R> a) {
+  using C = cplx<R>;
+  using Sh = KzRegShape<R, N>;
+  using Plan = typename Sh::Plan;
+  constexpr int P = Sh::P, E = Sh::E, LP = Sh::LP, CS = Sh::CS;
+  constexpr int NBL = N / (Plan::template radix<Plan::NPASS - 1>() * P);
+  const Geo g = a.g;
+  const int K = g.K, Hz = g.Hz;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  const int t = threadIdx.x % P, lp = threadIdx.x / P;
+  C* xcol = tw + N + lp * Sh::per_pair;
+  C* stg = xcol + CS;  // [6][2][Hz]: rows (x, y0), (x, y0+1) of each input field
+  const int pair = blockIdx.x * LP + lp, run = blockIdx.y;
+  const int x = pair / (N / 2), y0 = 2 * (pair % (N / 2));
+  const long long row0 = ((long long)x * N + y0) * Hz;
+  const C* yin = a.in + (long long)run * 6 * g.sY;
+  C* zout = a.out + (long long)run * 3 * g.sY;
+  // stage the 2 x Hz contiguous values of every field (16-byte aligned: Hz % 4 == 0),
+  // one commit group per field so that transform f waits only for its own rows
+  {
+    const int chunks = Hz;  // 2 * Hz complex = Hz 16-byte chunks
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      const C* src = yin + f * g.sY + row0;
+      C* dst = stg + f * 2 * Hz;
+      for (int c = t; c < chunks; c += P) cp_async16(dst + 2 * c, src + 2 * c);
+      cp_async_commit();
+    }
+  }
+  build_twiddles<Plan>(tw, a.tw, threadIdx.x, Sh::NT);
+  __syncthreads();
+  const WarpSync ws;
+
+  // Z = A + iB for rows (x, y0), (x, y0+1); kz > K is zero, kz < 0 by Hermitian symmetry
+  auto packed = [&](const C* fld) {
+    return [=](int k, int) -> C {
+      if (k <= K) {
+        C A = fld[k], B = fld[Hz + k];
+        if (k == 0) { A.y = 0; B.y = 0; }
+        return mk<C>(A.x - B.y, A.y + B.x);
+      }
+      if (k >= N - K) {
+        const C A = fld[N - k], B = fld[Hz + (N - k)];
+        return mk<C>(A.x + B.y, B.x - A.y);
+      }
+      return czero<C>();
+    };
+  };
+  // wait for field f's rows (5 - f later groups may still be in flight)
+  auto ready = [&](auto f_tag) {
+    constexpr int F_ = decltype(f_tag)::value;
+    cp_async_wait<5 - F_>();
+    __syncwarp();
+  };
+
+  C u[3][E], m[3][E], z[E];
+  auto inv_u = [&](auto c_tag) {
+    constexpr int c = decltype(c_tag)::value;
+    ready(c_tag);
+    auto src = packed(stg + c * 2 * Hz);
+    auto dst = [&](int b, int r, int, C v) { u[c][b + r * NBL] = v; };
+    fft_column<Plan, +1, Sh::PSH>(t, src, dst, xcol, tw, ws);
+  };
+  inv_u(std::integral_constant<int, 0>());
+  inv_u(std::integral_constant<int, 1>());
+  inv_u(std::integral_constant<int, 2>());
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int q = 0; q < E; ++q) m[c][q] = czero<C>();
+  // m = u x omega, one vorticity component at a time (lines packed in .x / .y)
+  auto inv_w = [&](auto w_tag) {
+    constexpr int w = decltype(w_tag)::value;
+    ready(std::integral_constant<int, 3 + w>());
+    auto src = packed(stg + (3 + w) * 2 * Hz);
+    auto dst = [&](int b, int r, int, C v) { z[b + r * NBL] = v; };
+    fft_column<Plan, +1, Sh::PSH>(t, src, dst, xcol, tw, ws);
+    constexpr int c1 = (w + 1) % 3, c2 = (w + 2) % 3;
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      m[c1][q] = mk<C>(m[c1][q].x + u[c2][q].x * z[q].x, m[c1][q].y + u[c2][q].y * z[q].y);
+      m[c2][q] = mk<C>(m[c2][q].x - u[c1][q].x * z[q].x, m[c2][q].y - u[c1][q].y * z[q].y);
+    }
+  };
+  inv_w(std::integral_constant<int, 0>());
+  inv_w(std::integral_constant<int, 1>());
+  inv_w(std::integral_constant<int, 2>());
+  // forward transforms straight from the registers, Hermitian unpack by shuffle
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    auto src = [&](int, int q) -> C { return m[c][q]; };
+    auto dst = [&](int b, int r, int, C v) { z[b + r * NBL] = v; };
+    fft_column<Plan, -1, Sh::PSH>(t, src, dst, xcol, tw, ws);
+    // partner value Z(N-k) for k = t + P q: lane (P-t) mod P, slot E-1-q (t != 0) or
+    // this lane, slot (E-q) mod E (t == 0)
+    C zm[E];
+    const int src_lane = (P - t) % P;
+#pragma unroll
+    for (int qq = 0; qq < E; ++qq) {
+      C v;
+      v.x = __shfl_sync(0xffffffffu, z[qq].x, src_lane, P);
+      v.y = __shfl_sync(0xffffffffu, z[qq].y, src_lane, P);
+      zm[E - 1 - qq] = (t != 0) ? v : z[(qq + 1) % E];
+    }
+    C* outf = zout + c * g.sY + row0;
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      const int k = t + P * q;
+      if (k <= K) {
+        outf[k] = mk<C>((z[q].x + zm[q].x) * R(0.5), (z[q].y - zm[q].y) * R(0.5));
+        outf[Hz + k] = mk<C>((z[q].y + zm[q].y) * R(0.5), (zm[q].x - z[q].x) * R(0.5));
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ x pass
+template <typename R, int N>
+struct KxRegShape {
+  using Plan = typename RegPlan<N>::T;
+  static constexpr int P = Plan::P, E = Plan::E;
+  static constexpr int QW = 4;                      // kz columns per group (one 32-byte sector)
+  static constexpr int GT = QW * P;                 // threads per group
+  static constexpr int NG = (GT >= 256) ? 1 : 256 / GT;
+  static constexpr int NT = NG * GT;
+  static constexpr int PSH = 3;
+  static constexpr int CS = ColLayout<N, PSH, 4>::CS;
+  static constexpr int MMAX = 2 * (N / 3) + 1;
+  // per group: state and accumulator tiles [2][3][M][QW], staged by cp.async
+  static constexpr long long stage_elems = 2LL * 3 * MMAX * QW;
+  static constexpr long long smem =
+      (long long)sizeof(cplx<R>) * (N + (long long)NG * QW * CS + (long long)NG * stage_elems);
+};
+
+
+
+// one of the six inverse-transformed fields u, curl u from the column's state
+template <int GI, typename C>
+__device__ __forceinline__ C uw_field(const C (&v)[3][RegPlan<256>::T::E], int q, float kx, float ky, float kz) {
+  if constexpr (GI < 3) {
+    return v[GI][q];
+  } else {
+    return curl_comp(GI - 3, v[0][q], v[1][q], v[2][q], kx, ky, kz);
+  }
+}
+
+template <typename R, int N, int MODE>
+__global__ void __launch_bounds__(KxRegShape<R, N>::NT) kx_reg_kernel(const PassArgs<R> a) {
+  using C = cplx<R>;
+  using Sh = KxRegShape<R, N>;
+  using Plan = typename Sh::Plan;
+  constexpr int P = Sh::P, E = Sh::E, QW = Sh::QW, GT = Sh::GT, CS = Sh::CS;
+  constexpr int NBL = N / (Plan::template radix<Plan::NPASS - 1>() * P);
+  static_assert(E == RegPlan<256>::T::E, "register plans hold 8 values per thread");
+  const Geo g = a.g;
+  const int K = g.K, M = g.M, Hz = g.Hz;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  const int grp = threadIdx.x / GT, lt = threadIdx.x % GT;
+  const int col = lt % QW, t = lt / QW;
+  const int iyc = blockIdx.x, run = blockIdx.z;
+  const int kz0 = (blockIdx.y * Sh::NG + grp) * QW;
+  const int kz = kz0 + col;
+  const bool zok = kz < g.Hk;
+  C* xcol = tw + N + (grp * QW + col) * CS;
+  // [0] state, [1] accumulator: [3][M][QW] each
+  C* stg = tw + N + Sh::NG * QW * CS + grp * Sh::stage_elems;
+  if constexpr (MODE == KX_STAGE) {
+    // stage the state (and accumulator) tiles of this group while the forward
+    // transforms run: rows of QW consecutive kz are 32-byte aligned (Hz % 4 == 0)
+    // and lie inside the padded rows (kz0 + QW <= Hz) whenever kz0 < Hk
+    if (kz0 < g.Hk) {
+      const int narr = (a.stage > 1) ? 2 : 1;
+      const long long base = (long long)blockIdx.z * 3 * g.sS + (long long)iyc * Hz + kz0;
+      const int chunks = narr * 3 * M * 2;  // 16-byte halves of each 32-byte row
+      for (int c = lt; c < chunks; c += GT) {
+        const int half = c & 1, row = c >> 1;  // row = (arr * 3 + f) * M + ic
+        const int arr = row / (3 * M), fi = row % (3 * M);
+        const C* src = (arr == 0 ? a.S : a.acc) + base + (long long)fi * M * Hz + 2 * half;
+        cp_async16(stg + (long long)row * QW + 2 * half, src);
+      }
+    }
+    cp_async_commit();
+  }
+  build_twiddles<Plan>(tw, a.tw, threadIdx.x, Sh::NT);
+  __syncthreads();
+  const float kyf = float(ksigned(iyc, K)), kzf = float(kz);
+  const long long soff = (long long)run * 3 * g.sS + (long long)iyc * Hz + kz;  // + (f*M + ic)*M*Hz
+
+  C v[3][E];
+  auto run_fft = [&](auto& src, auto& dst, auto dir_tag) {
+    constexpr int DIR = decltype(dir_tag)::value;
+    if constexpr (GT > 32) {
+      const NamedSync ns{1 + grp, GT};
+      fft_column<Plan, DIR, Sh::PSH>(t, src, dst, xcol, tw, ns);
+    } else {
+      const WarpSync ws;
+      fft_column<Plan, DIR, Sh::PSH>(t, src, dst, xcol, tw, ws);
+    }
+  };
+  using Fwd = std::integral_constant<int, -1>;
+  using Inv = std::integral_constant<int, +1>;
+
+  if constexpr (MODE == KX_LOAD) {
+    const C* sin_ = a.spec_in + soff;
+#pragma unroll
+    for (int f = 0; f < 3; ++f)
+#pragma unroll
+      for (int q = 0; q < E; ++q) {
+        const int ic = kcompact(t + P * q, N, K);
+        v[f][q] = (zok && ic >= 0) ? sin_[((long long)f * M + ic) * M * Hz] : czero<C>();
+      }
+  } else {
+    const R inv_n3 = R(1) / (R(N) * R(N) * R(N));
+    const C* win = a.in + (long long)run * 3 * g.sX + (long long)iyc * Hz + kz;
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      const C* wf = win + f * g.sX;
+      auto src = [&](int x, int) -> C { return zok ? wf[(long long)x * M * Hz] : czero<C>(); };
+      auto dst = [&](int b, int r, int, C val) { v[f][b + r * NBL] = cscale(val, inv_n3); };
+      run_fft(src, dst, Fwd());
+    }
+    // fused spectral pointwise stage on the modes k = t (mod P) of this column
+    cp_async_wait_all();
+    if constexpr (GT > 32) {
+      const NamedSync ns{1 + grp, GT};
+      ns();
+    } else {
+      __syncwarp();
+    }
+    const RunCoef cf = a.coef[run];
+    const bool expl = (a.flags & FLAG_EXPLICIT) != 0;
+    const R h = R(cf.dt);
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      const int ic = kcompact(t + P * q, N, K);
+      if (zok && ic >= 0) {
+        const float kx = float(ksigned(ic, K));
+        const float k2 = kx * kx + kyf * kyf + kzf * kzf;
+        leray(v[0][q], v[1][q], v[2][q], kx, kyf, kzf, k2);
+        const R lin = R(cf.nu * double(k2));
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+          const long long o = soff + ((long long)f * M + ic) * M * Hz;
+          const C s = stg[((long long)f * M + ic) * QW + col];
+          C acc = (a.stage > 1) ? stg[((long long)(3 + f) * M + ic) * QW + col] : czero<C>();
+          const C vs = (expl && a.stage > 1) ? a.vs[o] : s;
+          const C nv = rk4_combine<C>(a.stage, expl, v[f][q], s, acc, vs, h, lin);
+          if (a.stage < 4) {
+            a.acc[o] = acc;
+            if (expl) a.vs[o] = nv;
+          } else {
+            a.S[o] = nv;
+          }
+          v[f][q] = nv;
+        }
+      } else {
+#pragma unroll
+        for (int f = 0; f < 3; ++f) v[f][q] = czero<C>();
+      }
+    }
+  }
+
+  // inverse-x of u and curl u straight from the registers
+  C* xo = a.out + (long long)run * 6 * g.sX + (long long)iyc * Hz + kz;
+  auto inverse = [&](auto gi_tag) {
+    constexpr int GI = decltype(gi_tag)::value;
+    auto src = [&](int k, int q) -> C {
+      const int ic = kcompact(k, N, K);
+      if (ic < 0) return czero<C>();
+      return uw_field<GI>(v, q, float(ksigned(ic, K)), kyf, kzf);
+    };
+    C* xg = xo + GI * g.sX;
+    auto dst = [&](int, int, int x, C val) {
+      if (zok) xg[(long long)x * M * Hz] = val;
+    };
+    run_fft(src, dst, Inv());
+  };
+  inverse(std::integral_constant<int, 0>());
+  inverse(std::integral_constant<int, 1>());
+  inverse(std::integral_constant<int, 2>());
+  inverse(std::integral_constant<int, 3>());
+  inverse(std::integral_constant<int, 4>());
+  inverse(std::integral_constant<int, 5>());
+}
+
+template <typename R, int N>
+static cudaError_t launch_kz_reg(const PassArgs<R>& a, int runs, cudaStream_t st) {
+  using Sh = KzRegShape<R, N>;
+  static cudaError_t attr = set_smem(kz_reg_kernel<R, N>, Sh::smem);
+  if (attr != cudaSuccess) return attr;
+  const int pairs = N * N / 2;
+  dim3 grid(pairs / Sh::LP, runs);
+  kz_reg_kernel<R, N><<<grid, Sh::NT, Sh::smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename R, int N, int MODE>
+static cudaError_t launch_kx_reg(const PassArgs<R>& a, int runs, cudaStream_t st) {
+  using Sh = KxRegShape<R, N>;
+  static cudaError_t attr = set_smem(kx_reg_kernel<R, N, MODE>, Sh::smem);
+  if (attr != cudaSuccess) return attr;
+  const int quads = (a.g.Hk + Sh::QW - 1) / Sh::QW;
+  dim3 grid(a.g.M, (quads + Sh::NG - 1) / Sh::NG, runs);
+  kx_reg_kernel<R, N, MODE><<<grid, Sh::NT, Sh::smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace tg

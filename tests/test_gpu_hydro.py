@@ -109,3 +109,21 @@ def test_batched_runs_are_independent():
         s1 = p1.initial_condition("taylor_green", seed=3 + r, pert_amp=1e-2, k0=4.0)
         p1.step(s1, dt=2e-3, nu=nu, nsteps=5)
         assert torch.equal(s1[0], sb[r])
+
+
+@pytest.mark.parametrize("N", [16, 32, 64, 128])
+def test_register_and_shared_memory_passes_agree(N, monkeypatch):
+    """The register-resident x/z passes and the shared-memory passes are two
+    implementations of the same step; they agree to FP32 round-off."""
+    import torch
+    plans = []
+    for variant in ("0", "1"):
+        monkeypatch.setenv("TG_PASS_VARIANT", variant)
+        p = _plan(N, "f32")
+        s = p.initial_condition("taylor_green", seed=9, pert_amp=0.05, k0=3.0)
+        p.step(s, dt=2e-3, nu=2e-3, nsteps=3)
+        plans.append(from_state(p, s)[0])
+        r = p.rhs(p.initial_condition("taylor_green", seed=9, pert_amp=0.05, k0=3.0), nu=2e-3)
+        plans.append(from_state(p, r)[0])
+    assert rel_l2(plans[0], plans[2]) < 2e-6
+    assert rel_l2(plans[1], plans[3]) < 2e-6
