@@ -44,6 +44,8 @@ def parse():
                     help="seconds of host time for the CPU legs")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the MHD 128^3 and 64-run ensemble measurements")
     return ap.parse_args()
 
 
@@ -63,6 +65,132 @@ def algorithmic_bytes(n, K=None, F=3, csize=8):
         # stage 4 writes S instead of acc: the mean over the 4 stages
         "kx_stage_hd" if F == 3 else "kx_stage_mhd": F * X + F * S + 0.75 * F * S + F * S + G * X,
     }
+
+
+def measure_mhd(steps=100, n=128):
+    """MHD Taylor-Green 128^3 FP32, equal kinetic and magnetic energy, nu = eta = 1/800,
+    dt = 5e-4: RK4 steps/s and the per-pass profile."""
+    import torch
+
+    import jax_tg_project_gb300 as tg
+    plan = tg.Plan(n, physics="mhd", precision="f32")
+    s = plan.initial_condition("mhd_equal_energy")
+    plan.step(s, dt=5e-4, nu=1 / 800, eta=1 / 800, nsteps=3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    plan.step(s, dt=5e-4, nu=1 / 800, eta=1 / 800, nsteps=steps)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    d = plan.diagnostics(s).cpu().numpy()[0]
+    prof = plan.profile_passes(s, dt=5e-4, nu=1 / 800, eta=1 / 800, nsteps=2)
+    ab = algorithmic_bytes(n, F=6)
+    passes = {k: {"ms": m, "launches": c, "gbs": (ab[k] / (m * 1e-3) / 1e9) if k in ab else None}
+              for k, (m, c) in prof.items()}
+    return {"workload": f"mhd_taylor_green_{n}^3_fp32", "steps": steps, "steps_per_s": 1e3 / ms,
+            "ms_per_step": ms, "grid_point_updates_per_s": 1e3 / ms * n ** 3,
+            "hbm_step_bytes_model": step_bytes(n, F=6),
+            "step_gbs": step_bytes(n, F=6) / (ms * 1e-3) / 1e9,
+            "final": {"E_k": float(d[0]), "E_m": float(d[3]), "H_c": float(d[4])}, "passes": passes}
+
+
+def measure_ensemble(steps=50, count=64):
+    """64 independent hydro runs (N from {32,64,96}, Re log-uniform [100,3200], TG + 1e-3
+    perturbation, k0 = 4, dt = 1e-3, FP32): aggregate point updates/s batched vs one run at a time."""
+    import torch
+
+    import jax_tg_project_gb300 as tg
+    from jax_tg_project_gb300.ensemble import Ensemble, draw_runs
+    runs = draw_runs(count, seed=2024)
+    ens = Ensemble(runs, dt=1e-3, pert_amp=1e-3, k0=4.0, seed=7)
+    ens.step(3)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    ens.step(steps)
+    e1.record()
+    torch.cuda.synchronize()
+    t_b = e0.elapsed_time(e1) / 1e3
+    launches = ens.launches
+    singles = []
+    for r in runs:
+        p = tg.Plan(r.n)
+        st = p.initial_condition("taylor_green", seed=1, pert_amp=1e-3, k0=4.0)
+        p.step(st, dt=1e-3, nu=r.nu, nsteps=2)
+        singles.append((p, st, r))
+    torch.cuda.synchronize()
+    e0.record()
+    for p, st, r in singles:
+        p.step(st, dt=1e-3, nu=r.nu, nsteps=steps)
+    e1.record()
+    torch.cuda.synchronize()
+    t_s = e0.elapsed_time(e1) / 1e3
+    # per-size breakdown: one batched group alone, and one single run of that size
+    per_size = {}
+    for grp in ens.groups:
+        n = grp["n"]
+        e0.record()
+        grp["plan"].step(grp["state"], nsteps=steps)
+        e1.record()
+        torch.cuda.synchronize()
+        tb = e0.elapsed_time(e1) / steps
+        p, st, r = next(x for x in singles if x[2].n == n)
+        e0.record()
+        p.step(st, dt=1e-3, nu=r.nu, nsteps=steps)
+        e1.record()
+        torch.cuda.synchronize()
+        t1 = e0.elapsed_time(e1) / steps
+        per_size[n] = {"runs": len(grp["idx"]), "batched_ms_per_step": tb, "single_run_ms_per_step": t1,
+                       "batching_gain": len(grp["idx"]) * t1 / tb}
+    pts = sum(r.n ** 3 for r in runs) * steps
+    sizes = {n: sum(1 for r in runs if r.n == n) for n in sorted({r.n for r in runs})}
+    return {"workload": f"ensemble_{count}_runs_fp32", "runs_per_size": sizes, "steps": steps,
+            "batched_point_updates_per_s": pts / t_b, "sequential_point_updates_per_s": pts / t_s,
+            "batched_runs_steps_per_s": count * steps / t_b, "speedup_vs_sequential": t_s / t_b,
+            "batched_gpu_launches": launches, "per_size": per_size,
+            "note": "batched = one plan per size (all runs of a size per launch, per-run nu/dt), "
+                    "groups on concurrent streams, step graphs; sequential = one plan per run, "
+                    "run after run"}
+
+
+def measure_adjoint(n=128, nsteps=64):
+    """Gradient of the final enstrophy (128^3 FP32 hydro, TG + 1e-2 perturbation, nu = 1/1600,
+    dt = 1e-3): time of the hand-written adjoint (forward sweep with sqrt(n) checkpoints,
+    segment recompute, adjoint sweep) relative to the forward run, and its memory."""
+    import math
+
+    import torch
+
+    import jax_tg_project_gb300 as tg
+    plan = tg.Plan(n, precision="f32")
+    s0 = plan.initial_condition("taylor_green", seed=9, pert_amp=1e-2, k0=4.0)
+    s = s0.clone()
+    plan.step(s, dt=1e-3, nu=1 / 1600, nsteps=3)
+    ck = int(math.ceil(math.sqrt(nsteps)))
+    plan.adjoint(s0, 1e-3, 1 / 1600, 4, 2)  # warm-up
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s = s0.clone()
+    torch.cuda.synchronize()
+    e0.record()
+    plan.step(s, dt=1e-3, nu=1 / 1600, nsteps=nsteps)
+    e1.record()
+    torch.cuda.synchronize()
+    t_fwd = e0.elapsed_time(e1)
+    e0.record()
+    loss, grad, gnu = plan.adjoint(s0, 1e-3, 1 / 1600, nsteps, ck)
+    e1.record()
+    torch.cuda.synchronize()
+    t_adj = e0.elapsed_time(e1)
+    K = n // 3
+    M, Hz = 2 * K + 1, (K + 1 + 3) // 4 * 4
+    f = 3 * M * M * Hz * 8
+    work = (9 * n * M * Hz + 15 * n * n * Hz) * 8 + f * (18 + ck + (nsteps + ck - 1) // ck)
+    fwd_mem = plan.scratch_bytes + f
+    return {"workload": f"adjoint_final_enstrophy_{n}^3_fp32", "steps": nsteps, "checkpoint_every": ck,
+            "forward_ms": t_fwd, "adjoint_ms": t_adj, "time_ratio": t_adj / t_fwd,
+            "forward_bytes": fwd_mem, "adjoint_bytes": fwd_mem + work,
+            "memory_ratio": (fwd_mem + work) / fwd_mem, "loss": float(loss), "grad_nu": float(gnu)}
 
 
 def step_bytes(n, F=3, csize=8):
@@ -293,6 +421,11 @@ def run_ours(args, rank, world, local_rank):
                "sample": f"{len(times)} RK4 step(s) of the {n}^3 TG workload by the reference JAX "
                          "algorithm restated in NumPy/SciPy FP64, FFTs threaded over all cores"}
 
+    extras = None
+    if rank == 0 and not args.no_extras:
+        extras = {"mhd_128": measure_mhd(), "ensemble_64": measure_ensemble(),
+                  "adjoint_128": measure_adjoint()}
+
     clocks = clk.summary()
     if rank == 0:
         line = {
@@ -307,7 +440,7 @@ def run_ours(args, rank, world, local_rank):
             "step_gbs": step_alg / (ms_max / K * 1e-3) / 1e9,
             "step_frac_of_peak": step_alg / (ms_max / K * 1e-3) / 1e9 / peak,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clocks, "passes": passes,
+            "clocks": clocks, "passes": passes, "extras": extras,
         }
         print(json.dumps(line), flush=True)
 

@@ -186,6 +186,18 @@ int tg_profile_passes(tg_plan* plan, void* state, double dt, double nu, double e
 /* Kernels launched by the last tg_step / tg_run call (for launch accounting). */
 int64_t tg_last_launch_count(const tg_plan* plan);
 
+/* Discrete adjoint of nsteps integrating-factor RK4 steps (hydro, batch 1):
+ * loss = enstrophy of the final state (jax/taylor_green_jax.py:112-115 applied at
+ * t_final).  Writes loss (device double), grad_state = dloss/dstate0 (device, state
+ * layout; the gradient for the inner product sum_half w Re(a conj b), w = 1 at
+ * kz = 0 and 2 otherwise) and grad_nu = dloss/dnu (device double).  States are
+ * checkpointed every checkpoint_every steps (<= 0: ceil(sqrt(nsteps))) and each
+ * segment is recomputed once on the way back.  The reference has no adjoint; its
+ * autodiff counterpart is jax.grad through jax/taylor_green_jax.py:188-196.
+ * Allocates its work buffers for the call and synchronises the stream. */
+int tg_adjoint(tg_plan* plan, const void* state0, double dt, double nu, int nsteps, int checkpoint_every,
+               void* grad_state, double* grad_nu, double* loss);
+
 /* Allocation-free diagnostics.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory when they need the energies (a
  * framework that owns all device memory and forbids cudaMalloc inside its

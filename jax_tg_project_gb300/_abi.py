@@ -59,6 +59,8 @@ SIGNATURES = {
     "tg_physical_energy": (c_int, [c_void_p, c_void_p, c_void_p]),
     "tg_profile_passes": (c_int, [c_void_p, c_void_p, c_double, c_double, c_double, c_int,
                                   ctypes.POINTER(c_double), ctypes.POINTER(c_int64)]),
+    "tg_adjoint": (c_int, [c_void_p, c_void_p, c_double, c_double, c_int, c_int, c_void_p, c_void_p,
+                           c_void_p]),
     "tg_diagnostics_noalloc": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_double, c_double,
                                        c_void_p, c_void_p]),
     "tg_last_launch_count": (c_int64, [c_void_p]),

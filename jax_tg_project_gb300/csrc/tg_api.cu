@@ -28,7 +28,7 @@ TG_SIZES_F64(TG_DECL)
 
 enum PassOpHost {
   OP_KX_STAGE3 = 0, OP_KX_STAGE6, OP_KX_LOAD3, OP_KX_LOAD6, OP_KX_FWD3, OP_KX_FWD6,
-  OP_KY_INV, OP_KY_FWD, OP_KZ_PROD_HD, OP_KZ_PROD_MHD, OP_KZ_C2R, OP_KZ_R2C
+  OP_KY_INV, OP_KY_FWD, OP_KZ_PROD_HD, OP_KZ_PROD_MHD, OP_KZ_C2R, OP_KZ_R2C, OP_KZ_ADJ
 };
 
 template <typename R> using LaunchFn = cudaError_t (*)(int, const PassArgs<R>&, int, cudaStream_t);
@@ -342,6 +342,176 @@ __global__ void phys_energy_final(const double* part, int nblk, int groups, long
   Neumaier s;
   for (int b = 0; b < nblk; ++b) s.add(part[(long long)grp * nblk + b]);
   out[grp] = 0.5 * s.value() / double(n3);
+}
+
+// ------------------------------------------------------------------ adjoint pointwise kernels
+// All act on one run's compact fields [3][M][M][Hz]; k^2 from the mode index.
+struct ModeIdx {
+  int ic, iy, kz;
+  long long o;
+  double kx, ky, kzd, k2, w;
+};
+__device__ __forceinline__ bool mode_of(long long idx, const Geo& g, ModeIdx& m) {
+  const long long total = (long long)g.M * g.M * g.Hk;
+  if (idx >= total) return false;
+  m.kz = int(idx % g.Hk);
+  const long long r = idx / g.Hk;
+  m.iy = int(r % g.M);
+  m.ic = int(r / g.M);
+  m.o = ((long long)m.ic * g.M + m.iy) * g.Hz + m.kz;
+  m.kx = ksigned(m.ic, g.K);
+  m.ky = ksigned(m.iy, g.K);
+  m.kzd = m.kz;
+  m.k2 = m.kx * m.kx + m.ky * m.ky + m.kzd * m.kzd;
+  m.w = (m.kz == 0) ? 1.0 : 2.0;
+  return true;
+}
+
+// Lawson stage states: s = 2: E(h/2)(V + h/2 n); s = 3: E(h/2) V + h/2 n; s = 4: E(h) V + h E(h/2) n
+template <typename R>
+__global__ void lawson_stage_kernel(int s, const cplx<R>* V, const cplx<R>* n, cplx<R>* out, Geo g, double nu,
+                                    double h) {
+  ModeIdx m;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; mode_of(idx, g, m);
+       idx += (long long)gridDim.x * blockDim.x) {
+    const double lin = nu * m.k2;
+    const double m1 = expm1(-lin * h), mh = expm1(-0.5 * lin * h), eh = 1.0 + mh;
+    for (int f = 0; f < 3; ++f) {
+      const long long o = f * g.sS + m.o;
+      const double vx = V[o].x, vy = V[o].y, nx = n[o].x, ny = n[o].y;
+      double dx, dy;
+      if (s == 2) { dx = mh * vx + eh * 0.5 * h * nx; dy = mh * vy + eh * 0.5 * h * ny; }
+      else if (s == 3) { dx = mh * vx + 0.5 * h * nx; dy = mh * vy + 0.5 * h * ny; }
+      else { dx = m1 * vx + h * eh * nx; dy = m1 * vy + h * eh * ny; }
+      cplx<R> r;
+      r.x = R(vx + dx);
+      r.y = R(vy + dy);
+      out[o] = r;
+    }
+  }
+}
+
+// adjoint seeds of the stage nonlinear terms
+//   s = 4: mu = h/6 L;  s = 3: mu = h/3 E(h/2) L + h E(h/2) gp;  s = 2: mu = h/3 E(h/2) L + h/2 gp;
+//   s = 1: mu = h/6 E(h) L + h/2 E(h/2) gp   (L = adjoint of the step output, gp = previous stage adjoint)
+template <typename R>
+__global__ void adj_mu_kernel(int s, const cplx<R>* L, const cplx<R>* gp, cplx<R>* mu, Geo g, double nu, double h) {
+  ModeIdx m;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; mode_of(idx, g, m);
+       idx += (long long)gridDim.x * blockDim.x) {
+    const double lin = nu * m.k2;
+    const double e1 = exp(-lin * h), eh = exp(-0.5 * lin * h);
+    double cl, cg;
+    if (s == 4) { cl = h / 6.0; cg = 0.0; }
+    else if (s == 3) { cl = h / 3.0 * eh; cg = h * eh; }
+    else if (s == 2) { cl = h / 3.0 * eh; cg = 0.5 * h; }
+    else { cl = h / 6.0 * e1; cg = 0.5 * h * eh; }
+    for (int f = 0; f < 3; ++f) {
+      const long long o = f * g.sS + m.o;
+      double x = cl * double(L[o].x), y = cl * double(L[o].y);
+      if (s != 4) { x += cg * double(gp[o].x); y += cg * double(gp[o].y); }
+      cplx<R> r;
+      r.x = R(x);
+      r.y = R(y);
+      mu[o] = r;
+    }
+  }
+}
+
+// adjoint of the state at the start of the step:
+//   lam = E(h) L + E(h/2) (g2 + g3) + E(h) g4 + g1
+template <typename R>
+__global__ void adj_lambda_kernel(const cplx<R>* L, const cplx<R>* g1, const cplx<R>* g2, const cplx<R>* g3,
+                                  const cplx<R>* g4, cplx<R>* lam, Geo g, double nu, double h) {
+  ModeIdx m;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; mode_of(idx, g, m);
+       idx += (long long)gridDim.x * blockDim.x) {
+    const double lin = nu * m.k2;
+    const double e1 = exp(-lin * h), eh = exp(-0.5 * lin * h);
+    for (int f = 0; f < 3; ++f) {
+      const long long o = f * g.sS + m.o;
+      cplx<R> r;
+      r.x = R(e1 * (double(L[o].x) + double(g4[o].x)) + eh * (double(g2[o].x) + double(g3[o].x)) + double(g1[o].x));
+      r.y = R(e1 * (double(L[o].y) + double(g4[o].y)) + eh * (double(g2[o].y) + double(g3[o].y)) + double(g1[o].y));
+      lam[o] = r;
+    }
+  }
+}
+
+// d(loss)/d(nu) contribution of one step (block partial sums, FP64):
+//   <g2, -k^2 h/2 a2> + <g3, -k^2 h/2 E(h/2) V> + <g4, -k^2 h E(h) V - k^2 h^2/2 E(h/2) n3>
+//   + <L, -k^2 h E(h) V - k^2 h^2/6 (E(h) n1 + E(h/2) (n2 + n3))>,  <A,B> = sum_half w Re(A . conj B)
+template <typename R>
+__global__ void __launch_bounds__(kDiagThreads) adj_dnu_partial(const cplx<R>* L, const cplx<R>* V,
+                                                                const cplx<R>* a2, const cplx<R>* n1,
+                                                                const cplx<R>* n2, const cplx<R>* n3,
+                                                                const cplx<R>* g2, const cplx<R>* g3,
+                                                                const cplx<R>* g4, Geo g, double nu, double h,
+                                                                double* part) {
+  Neumaier q;
+  ModeIdx m;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; mode_of(idx, g, m);
+       idx += (long long)gridDim.x * blockDim.x) {
+    const double lin = nu * m.k2;
+    const double e1 = exp(-lin * h), eh = exp(-0.5 * lin * h);
+    const double kk = m.k2;
+    double acc = 0.0;
+    for (int f = 0; f < 3; ++f) {
+      const long long o = f * g.sS + m.o;
+      auto dot = [&](const cplx<R>* A, double bx, double by) { return double(A[o].x) * bx + double(A[o].y) * by; };
+      const double vx = V[o].x, vy = V[o].y;
+      acc += dot(g2, -kk * 0.5 * h * double(a2[o].x), -kk * 0.5 * h * double(a2[o].y));
+      acc += dot(g3, -kk * 0.5 * h * eh * vx, -kk * 0.5 * h * eh * vy);
+      acc += dot(g4, -kk * h * e1 * vx - kk * 0.5 * h * h * eh * double(n3[o].x),
+                 -kk * h * e1 * vy - kk * 0.5 * h * h * eh * double(n3[o].y));
+      acc += dot(L, -kk * h * e1 * vx - kk * h * h / 6.0 * (e1 * double(n1[o].x) + eh * (double(n2[o].x) + double(n3[o].x))),
+                 -kk * h * e1 * vy - kk * h * h / 6.0 * (e1 * double(n1[o].y) + eh * (double(n2[o].y) + double(n3[o].y))));
+    }
+    q.add(m.w * acc);
+  }
+  __shared__ double sh[kDiagThreads];
+  sh[threadIdx.x] = q.value();
+  __syncthreads();
+  for (int s = kDiagThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// acc += fixed-order compensated sum of nblk partials (single thread)
+__global__ void accumulate_partials(const double* part, int nblk, double* acc) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    Neumaier s;
+    for (int b = 0; b < nblk; ++b) s.add(part[b]);
+    *acc += s.value();
+  }
+}
+
+// gradient of the enstrophy 0.5 sum_half w |k x V|^2:  lam = k^2 V - k (k . V)
+template <typename R>
+__global__ void enstrophy_grad_kernel(const cplx<R>* V, cplx<R>* lam, Geo g) {
+  ModeIdx m;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; mode_of(idx, g, m);
+       idx += (long long)gridDim.x * blockDim.x) {
+    const double kv[3] = {m.kx, m.ky, m.kzd};
+    double dr = 0.0, di = 0.0;
+    for (int f = 0; f < 3; ++f) {
+      dr += kv[f] * double(V[f * g.sS + m.o].x);
+      di += kv[f] * double(V[f * g.sS + m.o].y);
+    }
+    for (int f = 0; f < 3; ++f) {
+      const long long o = f * g.sS + m.o;
+      cplx<R> r;
+      r.x = R(m.k2 * double(V[o].x) - kv[f] * dr);
+      r.y = R(m.k2 * double(V[o].y) - kv[f] * di);
+      lam[o] = r;
+    }
+  }
+}
+
+__global__ void copy_double(const double* src, double* dst) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *dst = *src;
 }
 }  // namespace tg
 
@@ -1042,3 +1212,208 @@ int tg_profile_passes(tg_plan* p, void* state, double dt, double nu, double eta,
 }
 
 }  // extern "C"
+
+// ====================================================================== adjoint
+namespace {
+
+template <typename R>
+struct Adjoint {
+  using C = cplx<R>;
+  tg_plan* p;
+  std::vector<void*> bufs;
+  size_t fbytes = 0;  // one 3-field compact array
+  C *X9 = nullptr, *Y9 = nullptr, *Z6 = nullptr, *WMU = nullptr;
+  C *cur = nullptr, *lam = nullptr, *lamn = nullptr, *mu = nullptr;
+  C *n1 = nullptr, *n2 = nullptr, *n3 = nullptr, *a2 = nullptr, *a3 = nullptr, *a4 = nullptr;
+  C *g1 = nullptr, *g2 = nullptr, *g3 = nullptr, *g4 = nullptr;
+  C *seg = nullptr, *ck = nullptr;
+  double* dnu = nullptr;
+  int blocks = 0;
+
+  ~Adjoint() {
+    for (void* b : bufs) cudaFree(b);
+  }
+  int alloc(void** ptr, size_t bytes) {
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      return fail(TG_E_NOMEM, std::string("tg_adjoint: cudaMalloc failed: ") + cudaGetErrorString(e));
+    }
+    bufs.push_back(*ptr);
+    return TG_OK;
+  }
+  int setup(int seglen, int nck) {
+    const Geo& g = p->g;
+    fbytes = sizeof(C) * 3 * (size_t)g.sS;
+    int rc;
+    struct { void** ptr; size_t bytes; } list[] = {
+        {(void**)&X9, sizeof(C) * 9 * (size_t)g.sX}, {(void**)&Y9, sizeof(C) * 9 * (size_t)g.sY},
+        {(void**)&Z6, sizeof(C) * 6 * (size_t)g.sY}, {(void**)&WMU, 2 * fbytes},
+        {(void**)&cur, fbytes}, {(void**)&lam, fbytes}, {(void**)&lamn, fbytes}, {(void**)&mu, fbytes},
+        {(void**)&n1, fbytes}, {(void**)&n2, fbytes}, {(void**)&n3, fbytes}, {(void**)&a2, fbytes},
+        {(void**)&a3, fbytes}, {(void**)&a4, fbytes}, {(void**)&g1, fbytes}, {(void**)&g2, fbytes},
+        {(void**)&g3, fbytes}, {(void**)&g4, fbytes}, {(void**)&seg, fbytes * (size_t)seglen},
+        {(void**)&ck, fbytes * (size_t)nck}, {(void**)&dnu, sizeof(double)}};
+    for (auto& b : list)
+      if ((rc = alloc(b.ptr, b.bytes))) return rc;
+    const long long modes = (long long)g.M * g.M * g.Hk;
+    blocks = (int)std::min<long long>((modes + 255) / 256, 2048);
+    return TG_OK;
+  }
+  int copy(C* dst, const C* src) {
+    TG_CUDA(cudaMemcpyAsync(dst, src, fbytes, cudaMemcpyDeviceToDevice, p->st), "adjoint copy");
+    return TG_OK;
+  }
+  // one RK4 step of X in place (eager launches, no graph)
+  int step(C* X) {
+    int rc;
+    if ((rc = Ops<R>::start(p, X))) return rc;
+    return Ops<R>::stages(p, X);
+  }
+  // out = P F[u x omega] of state X (no viscous term)
+  int nonlin(const C* X, C* out) {
+    int rc;
+    if ((rc = Ops<R>::start(p, X))) return rc;
+    if ((rc = Ops<R>::y_inv(p, p->G))) return rc;
+    if ((rc = Ops<R>::z_prod(p))) return rc;
+    if ((rc = Ops<R>::y_fwd(p, p->F))) return rc;
+    PassArgs<R> a = Ops<R>::base(p);
+    a.in = static_cast<const C*>(p->Y);
+    a.spec_out = out;
+    a.spec_in = X;
+    a.nin = 3;
+    a.flags |= FLAG_NONLIN;
+    return Ops<R>::go(p, OP_KX_FWD3, a, "kx nonlinear");
+  }
+  // out = N'(W)^T mu = F[omega x a] + i k x F[a x u],  a = F^-1 (P mu), (u, omega) of W
+  int nonlin_adj(const C* W, const C* m, C* out) {
+    int rc;
+    if ((rc = copy(WMU, W))) return rc;
+    if ((rc = copy(WMU + 3 * p->g.sS, m))) return rc;
+    PassArgs<R> a = Ops<R>::base(p);
+    a.spec_in = WMU;
+    a.out = X9;
+    a.map = MAP_ADJ;
+    a.nin = 6;
+    a.nout = 9;
+    if ((rc = Ops<R>::go(p, OP_KX_LOAD6, a, "kx adjoint load"))) return rc;
+    a = Ops<R>::base(p);
+    a.in = X9;
+    a.out = Y9;
+    a.nin = a.nout = 9;
+    if ((rc = Ops<R>::go(p, OP_KY_INV, a, "ky adjoint inverse"))) return rc;
+    a = Ops<R>::base(p);
+    a.in = Y9;
+    a.out = Z6;
+    a.nin = 9;
+    a.nout = 6;
+    if ((rc = Ops<R>::go(p, OP_KZ_ADJ, a, "kz adjoint"))) return rc;
+    a = Ops<R>::base(p);
+    a.in = Z6;
+    a.out = Y9;
+    a.nin = a.nout = 6;
+    if ((rc = Ops<R>::go(p, OP_KY_FWD, a, "ky adjoint forward"))) return rc;
+    a = Ops<R>::base(p);
+    a.in = Y9;
+    a.spec_out = out;
+    a.nin = 6;
+    a.flags |= FLAG_ADJ;
+    return Ops<R>::go(p, OP_KX_FWD6, a, "kx adjoint forward");
+  }
+  int launch_check(const char* what) {
+    TG_CUDA(cudaGetLastError(), what);
+    return TG_OK;
+  }
+  // lam_out = (d step / d V)^T lam_in at V; dnu += d(step)/d(nu) . lam_in
+  int step_adjoint(const C* V, const C* L, C* lam_out, double nu, double h) {
+    int rc;
+    const Geo& g = p->g;
+    cudaStream_t st = p->st;
+    if ((rc = nonlin(V, n1))) return rc;
+    lawson_stage_kernel<R><<<blocks, 256, 0, st>>>(2, V, n1, a2, g, nu, h);
+    if ((rc = launch_check("lawson stage"))) return rc;
+    if ((rc = nonlin(a2, n2))) return rc;
+    lawson_stage_kernel<R><<<blocks, 256, 0, st>>>(3, V, n2, a3, g, nu, h);
+    if ((rc = nonlin(a3, n3))) return rc;
+    lawson_stage_kernel<R><<<blocks, 256, 0, st>>>(4, V, n3, a4, g, nu, h);
+    adj_mu_kernel<R><<<blocks, 256, 0, st>>>(4, L, nullptr, mu, g, nu, h);
+    if ((rc = launch_check("adjoint seeds"))) return rc;
+    if ((rc = nonlin_adj(a4, mu, g4))) return rc;
+    adj_mu_kernel<R><<<blocks, 256, 0, st>>>(3, L, g4, mu, g, nu, h);
+    if ((rc = nonlin_adj(a3, mu, g3))) return rc;
+    adj_mu_kernel<R><<<blocks, 256, 0, st>>>(2, L, g3, mu, g, nu, h);
+    if ((rc = nonlin_adj(a2, mu, g2))) return rc;
+    adj_mu_kernel<R><<<blocks, 256, 0, st>>>(1, L, g2, mu, g, nu, h);
+    if ((rc = nonlin_adj(V, mu, g1))) return rc;
+    adj_lambda_kernel<R><<<blocks, 256, 0, st>>>(L, g1, g2, g3, g4, lam_out, g, nu, h);
+    adj_dnu_partial<R><<<kDiagBlocks, kDiagThreads, 0, st>>>(L, V, a2, n1, n2, n3, g2, g3, g4, g, nu, h, p->part);
+    accumulate_partials<<<1, 32, 0, st>>>(p->part, kDiagBlocks, dnu);
+    p->launches += 10;
+    return launch_check("adjoint combine");
+  }
+
+  int run(const void* state0, double dt, double nu, int nsteps, int seglen, void* grad, double* grad_nu,
+          double* loss) {
+    int rc;
+    const int nck = (nsteps + seglen - 1) / seglen;
+    if ((rc = setup(seglen, nck))) return rc;
+    cudaStream_t st = p->st;
+    const Geo& g = p->g;
+    // forward sweep, keeping the state at the start of every segment
+    if ((rc = copy(cur, static_cast<const C*>(state0)))) return rc;
+    for (int c = 0; c < nck; ++c) {
+      if ((rc = copy(ck + (size_t)c * 3 * g.sS, cur))) return rc;
+      const int len = std::min(seglen, nsteps - c * seglen);
+      for (int j = 0; j < len; ++j)
+        if ((rc = step(cur))) return rc;
+    }
+    // loss = enstrophy of the final state, and its gradient
+    if ((rc = Ops<R>::diagnostics(p, cur, p->dtmp))) return rc;
+    copy_double<<<1, 32, 0, st>>>(p->dtmp + TG_D_ENSTROPHY, loss);
+    enstrophy_grad_kernel<R><<<blocks, 256, 0, st>>>(cur, lam, g);
+    TG_CUDA(cudaMemsetAsync(dnu, 0, sizeof(double), st), "memset");
+    if ((rc = launch_check("loss gradient"))) return rc;
+    // backward sweep over the segments, recomputing each segment's states
+    for (int c = nck - 1; c >= 0; --c) {
+      const int len = std::min(seglen, nsteps - c * seglen);
+      if ((rc = copy(seg, ck + (size_t)c * 3 * g.sS))) return rc;
+      for (int j = 1; j < len; ++j) {
+        C* sj = seg + (size_t)j * 3 * g.sS;
+        if ((rc = copy(sj, sj - 3 * g.sS))) return rc;
+        if ((rc = step(sj))) return rc;
+      }
+      for (int j = len - 1; j >= 0; --j) {
+        if ((rc = step_adjoint(seg + (size_t)j * 3 * g.sS, lam, lamn, nu, dt))) return rc;
+        std::swap(lam, lamn);
+      }
+    }
+    TG_CUDA(cudaMemcpyAsync(grad, lam, fbytes, cudaMemcpyDeviceToDevice, st), "grad copy");
+    TG_CUDA(cudaMemcpyAsync(grad_nu, dnu, sizeof(double), cudaMemcpyDeviceToDevice, st), "grad_nu copy");
+    // the work buffers are freed on return: finish first
+    TG_CUDA(cudaStreamSynchronize(st), "adjoint sync");
+    return TG_OK;
+  }
+};
+
+}  // namespace
+
+extern "C" int tg_adjoint(tg_plan* p, const void* state0, double dt, double nu, int nsteps, int checkpoint_every,
+                          void* grad_state, double* grad_nu, double* loss) {
+  if (!p || !state0 || !grad_state || !grad_nu || !loss) return fail(TG_E_INVALID, "tg_adjoint: null argument");
+  if (p->F != 3 || p->batch != 1) return fail(TG_E_UNSUPPORTED, "tg_adjoint: hydro plans with batch 1 only");
+  if (!(dt > 0.0) || !(nu >= 0.0) || nsteps < 1)
+    return fail(TG_E_INVALID, "tg_adjoint: need dt > 0, nu >= 0 and nsteps >= 1");
+  if (p->flags & TG_FLAG_EXPLICIT_VISC)
+    return fail(TG_E_UNSUPPORTED, "tg_adjoint: differentiates the integrating-factor RK4 only");
+  int seglen = checkpoint_every > 0 ? checkpoint_every : (int)std::ceil(std::sqrt((double)nsteps));
+  seglen = std::max(1, std::min(seglen, nsteps));
+  int rc = set_coefs(p, dt, nu, 0.0);
+  if (rc) return rc;
+  p->launches = 0;
+  if (p->prec == TG_PREC_F64) {
+    Adjoint<double> A{p};
+    return A.run(state0, dt, nu, nsteps, seglen, grad_state, grad_nu, loss);
+  }
+  Adjoint<float> A{p};
+  return A.run(state0, dt, nu, nsteps, seglen, grad_state, grad_nu, loss);
+}

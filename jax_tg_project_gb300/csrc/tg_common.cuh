@@ -59,20 +59,26 @@ template <typename R, int N, int F> struct TileZ {
   static constexpr int value = (smem(base) <= 200 * 1024) ? base : base / 2;
 };
 
-// line pairs per CTA of the z pass
-template <typename R, int N> struct LinesZ {
+// line pairs per CTA of the z pass: the largest power of two <= pref that divides
+// the number of line pairs and keeps the CTA's shared memory (BUFS buffers of CS
+// complex values per pair, plus the twiddles) under 200 KiB
+template <typename R, int N, int BUFS = 7> struct LinesZ {
   static constexpr int P = PlanFor<N>::T::P;
   static constexpr int pref = (P >= 16) ? 8 : ((P >= 8) ? 16 : 32);
   static constexpr int pairs = N * N / 2;
-  // largest power of two <= pref dividing the number of line pairs
-  static constexpr int value = (pairs % pref == 0) ? pref
-      : (pairs % (pref / 2) == 0) ? pref / 2 : (pairs % (pref / 4) == 0) ? pref / 4 : 1;
+  static constexpr long long bytes(int lp) {
+    return (long long)sizeof(cplx<R>) * (N + (long long)lp * BUFS * ColLayout<N>::CS);
+  }
+  static constexpr int fit(int lp) {
+    return (lp <= 1) ? 1 : ((pairs % lp == 0 && bytes(lp) <= 200 * 1024) ? lp : fit(lp / 2));
+  }
+  static constexpr int value = fit(pref);
 };
 
 enum KxMode { KX_STAGE = 0, KX_LOAD = 1, KX_FWD = 2 };
-enum FieldMap { MAP_ID = 0, MAP_UW = 1, MAP_UWBJ = 2, MAP_DIV = 3, MAP_DIVB = 4, MAP_CURL = 5 };
-enum KzMode { KZ_PROD_HD = 0, KZ_PROD_MHD = 1, KZ_C2R = 2, KZ_R2C = 3 };
-enum Flags { FLAG_EXPLICIT = 1, FLAG_RHS = 2, FLAG_AMAX = 4 };
+enum FieldMap { MAP_ID = 0, MAP_UW = 1, MAP_UWBJ = 2, MAP_DIV = 3, MAP_DIVB = 4, MAP_CURL = 5, MAP_ADJ = 6 };
+enum KzMode { KZ_PROD_HD = 0, KZ_PROD_MHD = 1, KZ_C2R = 2, KZ_R2C = 3, KZ_ADJ = 4 };
+enum Flags { FLAG_EXPLICIT = 1, FLAG_RHS = 2, FLAG_AMAX = 4, FLAG_NONLIN = 8, FLAG_ADJ = 16 };
 
 template <typename R> struct PassArgs {
   Geo g;

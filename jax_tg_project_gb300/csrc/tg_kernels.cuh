@@ -50,6 +50,21 @@ __device__ __forceinline__ C field_value(int map, int gi, const C* sb, int ic, i
     }
     case MAP_CURL:
       return curl_comp(gi % 3, V(3 * (gi / 3)), V(3 * (gi / 3) + 1), V(3 * (gi / 3) + 2), kx, ky, kz);
+    case MAP_ADJ: {  // u, curl u of the state (fields 0..2) and the projected adjoint field (3..5)
+      if (gi < 3) return V(gi);
+      if (gi < 6) return curl_comp(gi - 3, V(0), V(1), V(2), kx, ky, kz);
+      C a = V(3), b = V(4), c = V(5);
+      const float k2 = kx * kx + ky * ky + kz * kz;
+      if (k2 > 0.f) {
+        const Re ik2 = Re(1) / Re(k2);
+        const Re dx = (Re(kx) * a.x + Re(ky) * b.x + Re(kz) * c.x) * ik2;
+        const Re dy = (Re(kx) * a.y + Re(ky) * b.y + Re(kz) * c.y) * ik2;
+        const Re kc = (gi == 6) ? Re(kx) : ((gi == 7) ? Re(ky) : Re(kz));
+        const C v = (gi == 6) ? a : ((gi == 7) ? b : c);
+        return mk<C>(v.x - kc * dx, v.y - kc * dy);
+      }
+      return (gi == 6) ? a : ((gi == 7) ? b : c);
+    }
     default:
       return czero<C>();
   }
@@ -169,6 +184,17 @@ kx_kernel(const PassArgs<R> a) {
       C n[F];
 #pragma unroll
       for (int f = 0; f < F; ++f) n[f] = sb[(f * M + ic) * TZ + c];
+      if constexpr (MODE == KX_FWD && F == 6) {
+        if (a.flags & FLAG_ADJ) {  // adjoint nonlinear term: F(omega x a) + i k x F(a x u)
+          C* so = a.spec_out + (long long)run * 3 * g.sS;
+#pragma unroll
+          for (int f = 0; f < 3; ++f) {
+            const C cq = curl_comp(f, n[3], n[4], n[5], kx, kyf, kzf);
+            so[f * g.sS + m0] = mk<C>(n[f].x + cq.x, n[f].y + cq.y);
+          }
+          continue;
+        }
+      }
       if constexpr (F == 6) {  // induction: i k x F(u x b), then projection (as the reference)
         C ex = n[3], ey = n[4], ez = n[5];
         n[3] = curl_comp(0, ex, ey, ez, kx, kyf, kzf);
@@ -179,10 +205,15 @@ kx_kernel(const PassArgs<R> a) {
       leray(n[0], n[1], n[2], kx, kyf, kzf, k2);
       if constexpr (MODE == KX_FWD) {
         C* so = a.spec_out + soff;
-        if (a.flags & FLAG_RHS) {  // RHS = P N - nu k^2 v  (v from spec_in)
+        if (a.flags & (FLAG_RHS | FLAG_NONLIN)) {  // RHS = P N - nu k^2 v (v from spec_in); P N alone
           const C* vi = a.spec_in + soff;
+          const bool visc = (a.flags & FLAG_NONLIN) == 0;
 #pragma unroll
           for (int f = 0; f < F; ++f) {
+            if (!visc) {
+              so[f * g.sS + m0] = n[f];
+              continue;
+            }
             const R lin = R((f < 3 ? cf.nu : cf.eta) * double(k2));
             const C v = vi[f * g.sS + m0];
             so[f * g.sS + m0] = mk<C>(n[f].x - lin * v.x, n[f].y - lin * v.y);
@@ -284,13 +315,13 @@ template <typename R, int N, int MODE>
 struct KzShape {
   using Plan = typename PlanFor<N>::T;
   static constexpr int P = Plan::P;
-  static constexpr int LP = LinesZ<R, N>::value;
   static constexpr int CS = ColLayout<N>::CS;
   // accumulate the cross products in registers (float) or shared memory (double)
   static constexpr bool ACC_REG = sizeof(R) == 4;
-  static constexpr int NPH = (MODE == KZ_PROD_HD) ? 3 : ((MODE == KZ_PROD_MHD) ? 6 : 0);
+  static constexpr int NPH = (MODE == KZ_PROD_HD) ? 3 : ((MODE == KZ_PROD_MHD || MODE == KZ_ADJ) ? 6 : 0);
   static constexpr int NACC = (MODE == KZ_C2R || MODE == KZ_R2C || ACC_REG) ? 0 : 3;
   static constexpr int BUFS = NPH + NACC + 1;  // + exchange column
+  static constexpr int LP = LinesZ<R, N, BUFS>::value;
   static constexpr long long smem = (long long)sizeof(cplx<R>) * (N + (long long)LP * BUFS * CS);
 };
 
@@ -342,7 +373,71 @@ kz_kernel(const PassArgs<R> a) {
     }
   };
 
-  if constexpr (MODE == KZ_PROD_HD || MODE == KZ_PROD_MHD) {
+  if constexpr (MODE == KZ_ADJ) {
+    // adjoint of u x omega: inputs u (0..2), omega (3..5), a (6..8); outputs
+    // p = omega x a (0..2) and q = a x u (3..5)
+    const C* yin = a.in + (long long)run * 9 * g.sY;
+    C* zout = a.out + (long long)run * 6 * g.sY;
+    C* ph = pbuf;  // u (0..2), a (3..5)
+    C zr[E];
+    C mr[Sh::ACC_REG ? 3 : 1][Sh::ACC_REG ? E : 1];
+    auto dst_reg = [&](int b, int r, int, C v) { zr[b * RL + r] = v; };
+    auto pt = [&](int e) { return out_index<Plan>(t, e / RL, e % RL); };
+    auto macc = [&](int c, int e) -> C& {
+      if constexpr (Sh::ACC_REG) return mr[c][e];
+      else return pbuf[(Sh::NPH + c) * CS + padx(pt(e))];
+    };
+    for (int c = 0; c < 6; ++c) {
+      const int fi = (c < 3) ? c : 3 + c;  // u -> 0..2, a -> 6..8
+      auto src = packed(yin + fi * g.sY);
+      fft_column<Plan, +1>(t, src, dst_reg, xcol, tw);
+#pragma unroll
+      for (int e = 0; e < E; ++e) ph[c * CS + padx(pt(e))] = zr[e];
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) macc(c, e) = czero<C>();
+    }
+#pragma unroll
+    for (int w = 0; w < 3; ++w) {  // (omega x a)_{w+1} -= omega_w a_{w+2};  (omega x a)_{w+2} += omega_w a_{w+1}
+      auto src = packed(yin + (3 + w) * g.sY);
+      fft_column<Plan, +1>(t, src, dst_reg, xcol, tw);
+      const int c1 = (w + 1) % 3, c2 = (w + 2) % 3;
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int n = padx(pt(e));
+        const C a1 = ph[(3 + c1) * CS + n], a2 = ph[(3 + c2) * CS + n];
+        const C om = zr[e];
+        C& p1 = macc(c1, e);
+        C& p2 = macc(c2, e);
+        p1 = mk<C>(p1.x - om.x * a2.x, p1.y - om.y * a2.y);
+        p2 = mk<C>(p2.x + om.x * a1.x, p2.y + om.y * a1.y);
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e) {  // q = a x u into 3..5, p into 0..2
+      const int n = padx(pt(e));
+      const C ux = ph[n], uy = ph[CS + n], uz = ph[2 * CS + n];
+      const C ax = ph[3 * CS + n], ay = ph[4 * CS + n], az = ph[5 * CS + n];
+      ph[3 * CS + n] = mk<C>(ay.x * uz.x - az.x * uy.x, ay.y * uz.y - az.y * uy.y);
+      ph[4 * CS + n] = mk<C>(az.x * ux.x - ax.x * uz.x, az.y * ux.y - ax.y * uz.y);
+      ph[5 * CS + n] = mk<C>(ax.x * uy.x - ay.x * ux.x, ax.y * uy.y - ay.y * ux.y);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) ph[c * CS + n] = macc(c, e);
+    }
+    __syncthreads();
+    for (int c = 0; c < 6; ++c) {
+      C* pc = ph + c * CS;
+      auto src = [&](int n, int) -> C { return pc[padx(n)]; };
+      fft_column<Plan, -1>(t, src, dst_reg, xcol, tw);
+      __syncthreads();
+#pragma unroll
+      for (int e = 0; e < E; ++e) pc[padx(pt(e))] = zr[e];
+      __syncthreads();
+      unpack_store(pc, zout + c * g.sY);
+    }
+  } else if constexpr (MODE == KZ_PROD_HD || MODE == KZ_PROD_MHD) {
     constexpr int F = (MODE == KZ_PROD_HD) ? 3 : 6;  // output fields
     const C* yin = a.in + (long long)run * (2 * F) * g.sY;
     C* zout = a.out + (long long)run * F * g.sY;
@@ -488,13 +583,16 @@ kz_kernel(const PassArgs<R> a) {
 // ------------------------------------------------------------------ launcher
 enum PassOp {
   OP_KX_STAGE3 = 0, OP_KX_STAGE6, OP_KX_LOAD3, OP_KX_LOAD6, OP_KX_FWD3, OP_KX_FWD6,
-  OP_KY_INV, OP_KY_FWD, OP_KZ_PROD_HD, OP_KZ_PROD_MHD, OP_KZ_C2R, OP_KZ_R2C, OP_COUNT
+  OP_KY_INV, OP_KY_FWD, OP_KZ_PROD_HD, OP_KZ_PROD_MHD, OP_KZ_C2R, OP_KZ_R2C, OP_KZ_ADJ, OP_COUNT
 };
 
 template <typename K>
 static cudaError_t set_smem(K kernel, long long bytes) {
-  if (bytes > 48 * 1024)
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (bytes > 48 * 1024) {
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) (void)cudaGetLastError();  // report through the return code only
+    return e;
+  }
   return cudaSuccess;
 }
 
@@ -507,7 +605,7 @@ static cudaError_t launch_kx(const PassArgs<R>& a, int runs, cudaStream_t st) {
   if (attr != cudaSuccess) return attr;
   dim3 grid(a.g.M, (a.g.Hk + TZ - 1) / TZ, runs);
   kx_kernel<R, N, F, MODE><<<grid, NT, smem, st>>>(a);
-  return cudaGetLastError();
+  return cudaGetLastError();  // also clears a launch-configuration error
 }
 
 template <typename R, int N, int DIR>
@@ -548,6 +646,7 @@ cudaError_t launch_pass(int op, const PassArgs<R>& a, int runs, cudaStream_t st)
     case OP_KZ_PROD_MHD: return launch_kz<R, N, KZ_PROD_MHD>(a, runs, st);
     case OP_KZ_C2R: return launch_kz<R, N, KZ_C2R>(a, runs, st);
     case OP_KZ_R2C: return launch_kz<R, N, KZ_R2C>(a, runs, st);
+    case OP_KZ_ADJ: return launch_kz<R, N, KZ_ADJ>(a, runs, st);
     default: return cudaErrorInvalidValue;
   }
 }

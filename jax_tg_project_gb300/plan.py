@@ -226,6 +226,17 @@ class Plan:
         check(self.lib.tg_physical_energy(self._h, _ptr(phys), _ptr(out)))
         return out
 
+    def adjoint(self, state0, dt, nu, nsteps, checkpoint_every=0):
+        """(loss, grad_state, grad_nu) of loss = final enstrophy after nsteps steps."""
+        self._check_state(state0)
+        grad = self.new_state()
+        out = torch.zeros(2, dtype=torch.float64, device=self.device)  # grad_nu, loss
+        self._sync_stream()
+        check(self.lib.tg_adjoint(self._h, _ptr(state0), float(dt), float(nu), int(nsteps),
+                                  int(checkpoint_every), _ptr(grad), ctypes.c_void_p(out.data_ptr()),
+                                  ctypes.c_void_p(out.data_ptr() + 8)))
+        return out[1], grad, out[0]
+
     def absmax(self, state, which="velocity"):
         self._check_state(state)
         sel = _abi.TG_ABSMAX_VELOCITY if which == "velocity" else _abi.TG_ABSMAX_DIVERGENCE

@@ -127,3 +127,19 @@ def test_register_and_shared_memory_passes_agree(N, monkeypatch):
         plans.append(from_state(p, r)[0])
     assert rel_l2(plans[0], plans[2]) < 2e-6
     assert rel_l2(plans[1], plans[3]) < 2e-6
+
+
+def test_fp32_step_tracks_fp64_gpu_run_at_256():
+    """The 256^3 throughput workload checked against an FP64 GPU run of the same steps."""
+    p32 = _plan(256, "f32")
+    p64 = _plan(256, "f64")
+    s32 = p32.initial_condition("taylor_green")
+    s64 = p64.initial_condition("taylor_green")
+    d32 = p32.run(s32, dt=2.5e-4, nu=1 / 1600, nsteps=20, save_every=10).cpu().numpy()[:, 0]
+    d64 = p64.run(s64, dt=2.5e-4, nu=1 / 1600, nsteps=20, save_every=10).cpu().numpy()[:, 0]
+    for col in (0, 1, 2):  # energy, enstrophy, dissipation
+        np.testing.assert_allclose(d32[:, col], d64[:, col], rtol=1e-6)
+    a = from_state(p32, s32)[0]
+    b = from_state(p64, s64)[0]
+    assert rel_l2(a, b) < 1e-5
+    del p32, p64
