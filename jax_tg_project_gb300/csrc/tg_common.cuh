@@ -41,7 +41,7 @@ template <> struct PlanFor<24> { using T = FftPlan<24, 2, 2, 12>; };
 template <> struct PlanFor<32> { using T = FftPlan<32, 4, 8, 4>; };
 template <> struct PlanFor<48> { using T = FftPlan<48, 4, 4, 12>; };
 template <> struct PlanFor<64> { using T = FftPlan<64, 8, 8, 8>; };
-template <> struct PlanFor<96> { using T = FftPlan<96, 4, 8, 12>; };
+template <> struct PlanFor<96> { using T = FftPlan<96, 8, 4, 4, 6>; };
 template <> struct PlanFor<128> { using T = FftPlan<128, 8, 16, 8>; };
 template <> struct PlanFor<256> { using T = FftPlan<256, 16, 16, 16>; };
 template <> struct PlanFor<512> { using T = FftPlan<512, 16, 16, 32>; };

@@ -17,9 +17,12 @@
 
 namespace tg {
 cudaError_t TG_CAT(launch, TG_REAL, TG_N)(int op, const PassArgs<TG_REAL>& a, int runs, cudaStream_t st) {
-  if constexpr (std::is_same<TG_REAL, float>::value && HasRegPlan<TG_N>::value) {
+  if constexpr (std::is_same<TG_REAL, float>::value && HasRegZ<TG_N>::value) {
+    if (a.variant == 0 && op == OP_KZ_PROD_HD) return launch_kz_reg<TG_REAL, TG_N>(a, runs, st);
+    if (a.variant == 0 && op == OP_KZ_PROD_MHD) return launch_kz_reg_mhd<TG_REAL, TG_N>(a, runs, st);
+  }
+  if constexpr (std::is_same<TG_REAL, float>::value && HasRegX<TG_N>::value) {
     if (a.variant == 0) {
-      if (op == OP_KZ_PROD_HD) return launch_kz_reg<TG_REAL, TG_N>(a, runs, st);
       if (op == OP_KX_STAGE3) return launch_kx_reg<TG_REAL, TG_N, KX_STAGE>(a, runs, st);
       if (op == OP_KX_LOAD3 && a.map == MAP_UW && a.nin == 3 && a.nout == 6)
         return launch_kx_reg<TG_REAL, TG_N, KX_LOAD>(a, runs, st);

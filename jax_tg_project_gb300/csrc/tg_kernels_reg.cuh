@@ -32,9 +32,12 @@ template <> struct RegPlan<32> { using T = FftPlan<32, 4, 8, 4>; };
 template <> struct RegPlan<64> { using T = FftPlan<64, 8, 8, 8>; };
 template <> struct RegPlan<128> { using T = FftPlan<128, 16, 8, 2, 8>; };
 template <> struct RegPlan<256> { using T = FftPlan<256, 32, 8, 4, 8>; };
+template <> struct RegPlan<96> { using T = FftPlan<96, 8, 4, 4, 6>; };  // E = 12: x pass only
 
-// sizes with a register plan (N = 8 has fewer line pairs than one CTA holds)
-template <int N> struct HasRegPlan { static constexpr bool value = (N == 16 || N == 32 || N == 64 || N == 128 || N == 256); };
+// sizes with a register-resident z pass (E = 8; N = 8 has fewer line pairs than one
+// CTA holds) and with a register-resident x pass
+template <int N> struct HasRegZ { static constexpr bool value = (N == 16 || N == 32 || N == 64 || N == 128 || N == 256); };
+template <int N> struct HasRegX { static constexpr bool value = HasRegZ<N>::value || N == 96; };
 
 // 16-byte asynchronous global -> shared copy (L1 bypass) and its completion wait
 __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
@@ -179,6 +182,211 @@ __global__ void __launch_bounds__(128, 3) kz_reg_kernel(const PassArgs<R> a) {
   }
 }
 
+// ------------------------------------------------------------------ z pass, MHD
+// Twelve inverse transforms (u, omega, b, j) and six forward ones (m = u x omega +
+// s j x b, e = u x b) per line pair, products in registers:
+//   u, b -> registers; e = u x b transformed straight from them; b parked in shared
+//   memory; omega accumulates m += u x omega; b back; j accumulates m += s j x b.
+// Inputs u, b, omega are staged by cp.async; j is read directly.
+template <typename R, int N>
+struct KzRegMhdShape {
+  using Plan = typename RegPlan<N>::T;
+  static constexpr int P = Plan::P, E = Plan::E;
+  static constexpr int NT = 128;
+  static constexpr int LP = NT / P;
+  static constexpr int PSH = (N >= 64) ? 4 : 3;
+  static constexpr int CS = ColLayout<N, PSH, (N == 16) ? 2 : 4>::CS;
+  static constexpr int HZMAX = ((N / 3 + 1) + 3) / 4 * 4;
+  static constexpr int NSTAGE = 9;        // staging slots, in order of use: u (0..2), b (3..5), omega (6..8)
+  static constexpr int SS = 2 * HZMAX;     // complex values per slot (two rows of up to HZMAX)
+  // exchange column + staged rows; b parks in slots 0..5 once u and b are transformed
+  static constexpr long long per_pair = CS + (long long)NSTAGE * SS;
+  static constexpr long long smem = (long long)sizeof(cplx<R>) * (N + (long long)LP * per_pair);
+  static_assert(3 * E * P <= 6 * SS, "parked b must fit in the slots of u and b");
+};
+
+template <typename R, int N>
+__global__ void __launch_bounds__(128) kz_reg_mhd_kernel(const PassArgs<R> a) {
+  using C = cplx<R>;
+  using Sh = KzRegMhdShape<R, N>;
+  using Plan = typename Sh::Plan;
+  constexpr int P = Sh::P, E = Sh::E, LP = Sh::LP, CS = Sh::CS;
+  constexpr int NBL = N / (Plan::template radix<Plan::NPASS - 1>() * P);
+  const Geo g = a.g;
+  const int K = g.K, Hz = g.Hz;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  const int t = threadIdx.x % P, lp = threadIdx.x / P;
+  C* xcol = tw + N + lp * Sh::per_pair;
+  C* stg = xcol + CS;  // slot i at stg + i * SS
+  const int pair = blockIdx.x * LP + lp, run = blockIdx.y;
+  const int x = pair / (N / 2), y0 = 2 * (pair % (N / 2));
+  const long long row0 = ((long long)x * N + y0) * Hz;
+  const C* yin = a.in + (long long)run * 12 * g.sY;
+  C* zout = a.out + (long long)run * 6 * g.sY;
+  // stage in the order of use, slot i <- field 0,1,2 (u), 6,7,8 (b), 3,4,5 (omega);
+  // one commit group per slot
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    const int f = (i < 3) ? i : ((i < 6) ? i + 3 : i - 3);
+    const C* src = yin + f * g.sY + row0;
+    C* dst = stg + i * Sh::SS;
+    for (int c = t; c < Hz; c += P) cp_async16(dst + 2 * c, src + 2 * c);
+    cp_async_commit();
+  }
+  build_twiddles<Plan>(tw, a.tw, threadIdx.x, Sh::NT);
+  __syncthreads();
+  const WarpSync ws;
+  const R sl = R(a.coef[run].lorentz);
+
+  auto packed = [&](const C* fld) {
+    return [=](int k, int) -> C {
+      if (k <= K) {
+        C A = fld[k], B = fld[Hz + k];
+        if (k == 0) { A.y = 0; B.y = 0; }
+        return mk<C>(A.x - B.y, A.y + B.x);
+      }
+      if (k >= N - K) {
+        const C A = fld[N - k], B = fld[Hz + (N - k)];
+        return mk<C>(A.x + B.y, B.x - A.y);
+      }
+      return czero<C>();
+    };
+  };
+  auto packed_g = [&](const C* fld) {  // j: straight from global memory
+    return [=](int k, int) -> C {
+      if (k <= K) {
+        C A = fld[row0 + k], B = fld[row0 + Hz + k];
+        if (k == 0) { A.y = 0; B.y = 0; }
+        return mk<C>(A.x - B.y, A.y + B.x);
+      }
+      if (k >= N - K) {
+        const C A = fld[row0 + (N - k)], B = fld[row0 + Hz + (N - k)];
+        return mk<C>(A.x + B.y, B.x - A.y);
+      }
+      return czero<C>();
+    };
+  };
+  C z[E];
+  // forward transform of a register field given by src(q), Hermitian unpack, store field c
+  auto forward_store = [&](auto& src, int c) {
+    auto dst = [&](int b, int r, int, C v) { z[b + r * NBL] = v; };
+    fft_column<Plan, -1, Sh::PSH>(t, src, dst, xcol, tw, ws);
+    C zm[E];
+    const int src_lane = (P - t) % P;
+#pragma unroll
+    for (int qq = 0; qq < E; ++qq) {
+      C v;
+      v.x = __shfl_sync(0xffffffffu, z[qq].x, src_lane, P);
+      v.y = __shfl_sync(0xffffffffu, z[qq].y, src_lane, P);
+      zm[E - 1 - qq] = (t != 0) ? v : z[(qq + 1) % E];
+    }
+    C* outf = zout + c * g.sY + row0;
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      const int k = t + P * q;
+      if (k <= K) {
+        outf[k] = mk<C>((z[q].x + zm[q].x) * R(0.5), (z[q].y - zm[q].y) * R(0.5));
+        outf[Hz + k] = mk<C>((z[q].y + zm[q].y) * R(0.5), (zm[q].x - z[q].x) * R(0.5));
+      }
+    }
+  };
+
+  C u[3][E], b[3][E];
+  auto inv_to = [&](auto slot_tag, auto wait_tag, auto* dstarr) {
+    constexpr int SLOT = decltype(slot_tag)::value;
+    cp_async_wait<decltype(wait_tag)::value>();
+    __syncwarp();
+    auto src = packed(stg + SLOT * Sh::SS);
+    auto dst = [&](int bb, int r, int, C v) { dstarr[bb + r * NBL] = v; };
+    fft_column<Plan, +1, Sh::PSH>(t, src, dst, xcol, tw, ws);
+  };
+  using I0 = std::integral_constant<int, 0>;
+  using I1 = std::integral_constant<int, 1>;
+  using I2 = std::integral_constant<int, 2>;
+  inv_to(I0(), std::integral_constant<int, 8>(), u[0]);
+  inv_to(I1(), std::integral_constant<int, 7>(), u[1]);
+  inv_to(I2(), std::integral_constant<int, 6>(), u[2]);
+  inv_to(std::integral_constant<int, 3>(), std::integral_constant<int, 5>(), b[0]);
+  inv_to(std::integral_constant<int, 4>(), std::integral_constant<int, 4>(), b[1]);
+  inv_to(std::integral_constant<int, 5>(), std::integral_constant<int, 3>(), b[2]);
+  // e = u x b (output fields 3..5)
+  {
+    auto e0 = [&](int, int q) -> C { return mk<C>(u[1][q].x * b[2][q].x - u[2][q].x * b[1][q].x,
+                                                  u[1][q].y * b[2][q].y - u[2][q].y * b[1][q].y); };
+    auto e1 = [&](int, int q) -> C { return mk<C>(u[2][q].x * b[0][q].x - u[0][q].x * b[2][q].x,
+                                                  u[2][q].y * b[0][q].y - u[0][q].y * b[2][q].y); };
+    auto e2 = [&](int, int q) -> C { return mk<C>(u[0][q].x * b[1][q].x - u[1][q].x * b[0][q].x,
+                                                  u[0][q].y * b[1][q].y - u[1][q].y * b[0][q].y); };
+    forward_store(e0, 3);
+    forward_store(e1, 4);
+    forward_store(e2, 5);
+  }
+  // park b in slots 0..5 (every thread of the warp is past the reads of u and b)
+  __syncwarp();
+  C* park = stg;
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int q = 0; q < E; ++q) park[(c * E + q) * P + t] = b[c][q];
+  C m[3][E];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int q = 0; q < E; ++q) m[c][q] = czero<C>();
+  auto add_uw = [&](auto w_tag, auto wait_tag) {
+    constexpr int w = decltype(w_tag)::value;
+    inv_to(std::integral_constant<int, 6 + w>(), wait_tag, z);
+    constexpr int c1 = (w + 1) % 3, c2 = (w + 2) % 3;
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      m[c1][q] = mk<C>(m[c1][q].x + u[c2][q].x * z[q].x, m[c1][q].y + u[c2][q].y * z[q].y);
+      m[c2][q] = mk<C>(m[c2][q].x - u[c1][q].x * z[q].x, m[c2][q].y - u[c1][q].y * z[q].y);
+    }
+  };
+  add_uw(I0(), std::integral_constant<int, 2>());
+  add_uw(I1(), std::integral_constant<int, 1>());
+  add_uw(I2(), std::integral_constant<int, 0>());
+  __syncwarp();
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int q = 0; q < E; ++q) b[c][q] = park[(c * E + q) * P + t];
+  // m += s (j x b):  (j x b)_{w+1} -= j_w b_{w+2};  (j x b)_{w+2} += j_w b_{w+1}
+  auto add_jb = [&](auto w_tag) {
+    constexpr int w = decltype(w_tag)::value;
+    auto src = packed_g(yin + (9 + w) * g.sY);
+    auto dst = [&](int bb, int r, int, C v) { z[bb + r * NBL] = v; };
+    fft_column<Plan, +1, Sh::PSH>(t, src, dst, xcol, tw, ws);
+    constexpr int c1 = (w + 1) % 3, c2 = (w + 2) % 3;
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      m[c1][q] = mk<C>(m[c1][q].x - sl * z[q].x * b[c2][q].x, m[c1][q].y - sl * z[q].y * b[c2][q].y);
+      m[c2][q] = mk<C>(m[c2][q].x + sl * z[q].x * b[c1][q].x, m[c2][q].y + sl * z[q].y * b[c1][q].y);
+    }
+  };
+  add_jb(I0());
+  add_jb(I1());
+  add_jb(I2());
+  auto m0 = [&](int, int q) -> C { return m[0][q]; };
+  auto m1 = [&](int, int q) -> C { return m[1][q]; };
+  auto m2 = [&](int, int q) -> C { return m[2][q]; };
+  forward_store(m0, 0);
+  forward_store(m1, 1);
+  forward_store(m2, 2);
+}
+
+template <typename R, int N>
+static cudaError_t launch_kz_reg_mhd(const PassArgs<R>& a, int runs, cudaStream_t st) {
+  using Sh = KzRegMhdShape<R, N>;
+  static cudaError_t attr = set_smem(kz_reg_mhd_kernel<R, N>, Sh::smem);
+  if (attr != cudaSuccess) return attr;
+  const int pairs = N * N / 2;
+  dim3 grid(pairs / Sh::LP, runs);
+  kz_reg_mhd_kernel<R, N><<<grid, Sh::NT, Sh::smem, st>>>(a);
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ x pass
 template <typename R, int N>
 struct KxRegShape {
@@ -186,7 +394,8 @@ struct KxRegShape {
   static constexpr int P = Plan::P, E = Plan::E;
   static constexpr int QW = 4;                      // kz columns per group (one 32-byte sector)
   static constexpr int GT = QW * P;                 // threads per group
-  static constexpr int NG = (GT >= 256) ? 1 : 256 / GT;
+  static constexpr int TARGET = (P >= 16) ? 256 : 128;  // threads per CTA
+  static constexpr int NG = (GT >= TARGET) ? 1 : TARGET / GT;
   static constexpr int NT = NG * GT;
   static constexpr int PSH = 3;
   static constexpr int CS = ColLayout<N, PSH, 4>::CS;
@@ -200,8 +409,8 @@ struct KxRegShape {
 
 
 // one of the six inverse-transformed fields u, curl u from the column's state
-template <int GI, typename C>
-__device__ __forceinline__ C uw_field(const C (&v)[3][RegPlan<256>::T::E], int q, float kx, float ky, float kz) {
+template <int GI, typename C, int E>
+__device__ __forceinline__ C uw_field(const C (&v)[3][E], int q, float kx, float ky, float kz) {
   if constexpr (GI < 3) {
     return v[GI][q];
   } else {
@@ -216,7 +425,6 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT) kx_reg_kernel(const Pass
   using Plan = typename Sh::Plan;
   constexpr int P = Sh::P, E = Sh::E, QW = Sh::QW, GT = Sh::GT, CS = Sh::CS;
   constexpr int NBL = N / (Plan::template radix<Plan::NPASS - 1>() * P);
-  static_assert(E == RegPlan<256>::T::E, "register plans hold 8 values per thread");
   const Geo g = a.g;
   const int K = g.K, M = g.M, Hz = g.Hz;
   extern __shared__ __align__(16) unsigned char smem_raw[];

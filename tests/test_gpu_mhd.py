@@ -97,3 +97,16 @@ def test_mhd_run_matches_reference_run(golden_cupy):
     np.testing.assert_allclose(series[:, 4], g["mhdrun8_cross_helicities"], rtol=1e-6)
     np.testing.assert_allclose(series[:, 1], g["mhdrun8_enstrophies"], rtol=1e-6)
     assert series[:, 6].max() < 1e-4 and series[:, 7].max() < 1e-4
+
+
+@pytest.mark.parametrize("N", [16, 32, 64, 128])
+def test_mhd_register_and_shared_memory_passes_agree(N, monkeypatch):
+    """Register-resident MHD z pass against the shared-memory one (FP32 round-off)."""
+    outs = []
+    for variant in ("0", "1"):
+        monkeypatch.setenv("TG_PASS_VARIANT", variant)
+        p = _plan(N, "f32")
+        s = p.initial_condition("mhd_equal_energy", seed=2, pert_amp=0.05, k0=3.0)
+        p.step(s, dt=1e-3, nu=2e-3, eta=3e-3, nsteps=3)
+        outs.append(from_state(p, s)[0])
+    assert rel_l2(outs[0], outs[1]) < 2e-6
