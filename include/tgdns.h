@@ -198,6 +198,13 @@ int64_t tg_last_launch_count(const tg_plan* plan);
 int tg_adjoint(tg_plan* plan, const void* state0, double dt, double nu, int nsteps, int checkpoint_every,
                void* grad_state, double* grad_nu, double* loss);
 
+/* Shell-summed energy spectrum E(k) = 0.5 sum_{round(|k|) = k} |u_k|^2 (full-spectrum sum)
+ * for k = 0 .. tg_spectrum_bins(plan)-1, per run into out (device doubles,
+ * [batch][bins] for hydro, [batch][2][bins] (kinetic, magnetic) for MHD).  Not in the
+ * reference (a natural extension of its diagnostics); deterministic summation order. */
+int tg_spectrum_bins(const tg_plan* plan);
+int tg_energy_spectrum(tg_plan* plan, const void* state, double* out);
+
 /* Allocation-free diagnostics.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory when they need the energies (a
  * framework that owns all device memory and forbids cudaMalloc inside its

@@ -61,6 +61,8 @@ SIGNATURES = {
                                   ctypes.POINTER(c_double), ctypes.POINTER(c_int64)]),
     "tg_adjoint": (c_int, [c_void_p, c_void_p, c_double, c_double, c_int, c_int, c_void_p, c_void_p,
                            c_void_p]),
+    "tg_spectrum_bins": (c_int, [c_void_p]),
+    "tg_energy_spectrum": (c_int, [c_void_p, c_void_p, c_void_p]),
     "tg_diagnostics_noalloc": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_double, c_double,
                                        c_void_p, c_void_p]),
     "tg_last_launch_count": (c_int64, [c_void_p]),

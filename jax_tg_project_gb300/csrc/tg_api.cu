@@ -513,6 +513,61 @@ __global__ void enstrophy_grad_kernel(const cplx<R>* V, cplx<R>* lam, Geo g) {
 __global__ void copy_double(const double* src, double* dst) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *dst = *src;
 }
+
+// shell-summed energy spectrum E(k) = 0.5 sum_{round|k| = k} w |u_k|^2: per-block partial
+// histograms in shared memory (fixed order inside a block), then a fixed-order sum over blocks
+constexpr int kSpecBlocks = 64;
+template <typename R>
+__global__ void __launch_bounds__(256) spectrum_partial(const cplx<R>* S, Geo g, int F, int nbins, double* part) {
+  extern __shared__ double hist[];
+  const int run = blockIdx.y;
+  const cplx<R>* base = S + (long long)run * F * g.sS;
+  for (int i = threadIdx.x; i < 2 * nbins; i += blockDim.x) hist[i] = 0.0;
+  __syncthreads();
+  const long long total = (long long)g.M * g.M * g.Hk;
+  // each thread owns a contiguous chunk; bins accumulate thread by thread in order
+  const long long per_block = (total + gridDim.x - 1) / gridDim.x;
+  const long long b0 = (long long)blockIdx.x * per_block, b1 = min(total, b0 + per_block);
+  for (int tt = 0; tt < blockDim.x; ++tt) {
+    // serialise the threads of a block so that the per-bin order is fixed
+    if (threadIdx.x == tt) {
+      for (long long idx = b0 + tt; idx < b1; idx += blockDim.x) {
+        const int kz = int(idx % g.Hk);
+        const long long r = idx / g.Hk;
+        const int iyc = int(r % g.M), ic = int(r / g.M);
+        const double kx = ksigned(ic, g.K), ky = ksigned(iyc, g.K);
+        const int bin = int(floor(sqrt(kx * kx + ky * ky + double(kz) * kz) + 0.5));
+        const double w = (kz == 0) ? 1.0 : 2.0;
+        const long long o = ((long long)ic * g.M + iyc) * g.Hz + kz;
+        double eu = 0.0, eb = 0.0;
+        for (int f = 0; f < 3; ++f) {
+          const cplx<R> v = base[f * g.sS + o];
+          eu += double(v.x) * v.x + double(v.y) * v.y;
+          if (F == 6) {
+            const cplx<R> b = base[(3 + f) * g.sS + o];
+            eb += double(b.x) * b.x + double(b.y) * b.y;
+          }
+        }
+        if (bin < nbins) {
+          hist[bin] += 0.5 * w * eu;
+          hist[nbins + bin] += 0.5 * w * eb;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < 2 * nbins; i += blockDim.x)
+    part[((long long)run * gridDim.x + blockIdx.x) * 2 * nbins + i] = hist[i];
+}
+
+__global__ void spectrum_final(const double* part, int nblk, int nbins, int F, double* out) {
+  const int run = blockIdx.x;
+  for (int i = threadIdx.x; i < nbins * (F == 6 ? 2 : 1); i += blockDim.x) {
+    double s = 0.0;
+    for (int b = 0; b < nblk; ++b) s += part[((long long)run * nblk + b) * 2 * nbins + i];
+    out[(long long)run * nbins * (F == 6 ? 2 : 1) + i] = s;
+  }
+}
 }  // namespace tg
 
 // ====================================================================== plan
@@ -1416,4 +1471,31 @@ extern "C" int tg_adjoint(tg_plan* p, const void* state0, double dt, double nu, 
   }
   Adjoint<float> A{p};
   return A.run(state0, dt, nu, nsteps, seglen, grad_state, grad_nu, loss);
+}
+
+extern "C" int tg_spectrum_bins(const tg_plan* p) {
+  return p ? (int)std::floor(std::sqrt(3.0) * p->K + 0.5) + 1 : 0;
+}
+
+extern "C" int tg_energy_spectrum(tg_plan* p, const void* state, double* out) {
+  if (!p || !state || !out) return fail(TG_E_INVALID, "tg_energy_spectrum: null argument");
+  const int nbins = tg_spectrum_bins(p);
+  double* part = nullptr;
+  const size_t pbytes = sizeof(double) * (size_t)p->batch * kSpecBlocks * 2 * nbins;
+  cudaError_t e = cudaMallocAsync((void**)&part, pbytes, p->st);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return fail(TG_E_NOMEM, std::string("tg_energy_spectrum: ") + cudaGetErrorString(e));
+  }
+  dim3 grid(kSpecBlocks, p->batch);
+  const size_t shm = sizeof(double) * 2 * nbins;
+  if (p->prec == TG_PREC_F64)
+    spectrum_partial<double><<<grid, 256, shm, p->st>>>(static_cast<const cplx<double>*>(state), p->g, p->F, nbins, part);
+  else
+    spectrum_partial<float><<<grid, 256, shm, p->st>>>(static_cast<const cplx<float>*>(state), p->g, p->F, nbins, part);
+  spectrum_final<<<p->batch, 128, 0, p->st>>>(part, kSpecBlocks, nbins, p->F, out);
+  e = cudaGetLastError();
+  cudaFreeAsync(part, p->st);
+  if (e != cudaSuccess) return cuda_fail(e, "tg_energy_spectrum");
+  return TG_OK;
 }

@@ -237,6 +237,39 @@ class Plan:
                                   ctypes.c_void_p(out.data_ptr() + 8)))
         return out[1], grad, out[0]
 
+    def energy_spectrum(self, state):
+        """E(k) per run: (batch, bins) hydro or (batch, 2, bins) MHD (kinetic, magnetic)."""
+        self._check_state(state)
+        nb = int(self.lib.tg_spectrum_bins(self._h))
+        shape = (self.batch, nb) if self.F == 3 else (self.batch, 2, nb)
+        out = torch.zeros(shape, dtype=torch.float64, device=self.device)
+        self._sync_stream()
+        check(self.lib.tg_energy_spectrum(self._h, _ptr(state), _ptr(out)))
+        return out
+
+    def save(self, path, state, **meta):
+        """Write the state (compact coefficients, padding dropped) and metadata to an .npz file."""
+        import numpy as np
+        self._check_state(state)
+        np.savez_compressed(path, coefficients=state[..., : self.K + 1].cpu().numpy(), n=self.n,
+                            physics=self.physics, precision=self.precision, K=self.K,
+                            **{k: np.asarray(v) for k, v in meta.items()})
+
+    def load(self, path):
+        """Read a state written by ``save`` (same n, physics and cutoff); returns (state, meta)."""
+        import numpy as np
+        d = np.load(path, allow_pickle=False)
+        if int(d["n"]) != self.n or str(d["physics"]) != self.physics or int(d["K"]) != self.K:
+            raise ValueError(f"{path}: saved for n={int(d['n'])}, physics={d['physics']}, "
+                             f"K={int(d['K'])}; this plan is n={self.n}, physics={self.physics}")
+        c = d["coefficients"]
+        if c.shape[0] != self.batch:
+            raise ValueError(f"{path}: {c.shape[0]} runs saved, plan has batch {self.batch}")
+        s = self.new_state()
+        s[..., : self.K + 1] = torch.from_numpy(c).to(self.complex_dtype).to(self.device)
+        meta = {k: d[k] for k in d.files if k not in ("coefficients", "n", "physics", "precision", "K")}
+        return s, meta
+
     def absmax(self, state, which="velocity"):
         self._check_state(state)
         sel = _abi.TG_ABSMAX_VELOCITY if which == "velocity" else _abi.TG_ABSMAX_DIVERGENCE
