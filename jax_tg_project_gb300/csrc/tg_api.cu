@@ -28,8 +28,12 @@ TG_SIZES_F64(TG_DECL)
 
 enum PassOpHost {
   OP_KX_STAGE3 = 0, OP_KX_STAGE6, OP_KX_LOAD3, OP_KX_LOAD6, OP_KX_FWD3, OP_KX_FWD6,
-  OP_KY_INV, OP_KY_FWD, OP_KZ_PROD_HD, OP_KZ_PROD_MHD, OP_KZ_C2R, OP_KZ_R2C, OP_KZ_ADJ
+  OP_KY_INV, OP_KY_FWD, OP_KZ_PROD_HD, OP_KZ_PROD_MHD, OP_KZ_C2R, OP_KZ_R2C, OP_KZ_ADJ,
+  OP_KX_ADJ_LOAD, OP_KX_ADJ_FWD, OP_KX_NL_FWD
 };
+
+// sizes whose FP32 build has the register-resident adjoint x / z passes
+static bool has_reg_adjoint(int n) { return n == 16 || n == 32 || n == 64 || n == 128 || n == 256; }
 
 template <typename R> using LaunchFn = cudaError_t (*)(int, const PassArgs<R>&, int, cudaStream_t);
 
@@ -368,24 +372,31 @@ __device__ __forceinline__ bool mode_of(long long idx, const Geo& g, ModeIdx& m)
 }
 
 // Lawson stage states: s = 2: E(h/2)(V + h/2 n); s = 3: E(h/2) V + h/2 n; s = 4: E(h) V + h E(h/2) n
+// (working precision; factors applied in the expm1 delta form like the forward kernels)
+template <typename R> __device__ __forceinline__ R wexpm1(R x);
+template <> __device__ __forceinline__ float wexpm1<float>(float x) { return expm1f(x); }
+template <> __device__ __forceinline__ double wexpm1<double>(double x) { return expm1(x); }
+
 template <typename R>
 __global__ void lawson_stage_kernel(int s, const cplx<R>* V, const cplx<R>* n, cplx<R>* out, Geo g, double nu,
-                                    double h) {
+                                    double hd) {
   ModeIdx m;
+  const R h = R(hd);
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; mode_of(idx, g, m);
        idx += (long long)gridDim.x * blockDim.x) {
-    const double lin = nu * m.k2;
-    const double m1 = expm1(-lin * h), mh = expm1(-0.5 * lin * h), eh = 1.0 + mh;
+    const R lin = R(nu * m.k2);
+    const R m1 = wexpm1<R>(-lin * h), mh = wexpm1<R>(R(-0.5) * lin * h), eh = R(1) + mh;
+#pragma unroll
     for (int f = 0; f < 3; ++f) {
       const long long o = f * g.sS + m.o;
-      const double vx = V[o].x, vy = V[o].y, nx = n[o].x, ny = n[o].y;
-      double dx, dy;
-      if (s == 2) { dx = mh * vx + eh * 0.5 * h * nx; dy = mh * vy + eh * 0.5 * h * ny; }
-      else if (s == 3) { dx = mh * vx + 0.5 * h * nx; dy = mh * vy + 0.5 * h * ny; }
-      else { dx = m1 * vx + h * eh * nx; dy = m1 * vy + h * eh * ny; }
+      const cplx<R> v = V[o], nn = n[o];
+      R dx, dy;
+      if (s == 2) { dx = mh * v.x + eh * R(0.5) * h * nn.x; dy = mh * v.y + eh * R(0.5) * h * nn.y; }
+      else if (s == 3) { dx = mh * v.x + R(0.5) * h * nn.x; dy = mh * v.y + R(0.5) * h * nn.y; }
+      else { dx = m1 * v.x + h * eh * nn.x; dy = m1 * v.y + h * eh * nn.y; }
       cplx<R> r;
-      r.x = R(vx + dx);
-      r.y = R(vy + dy);
+      r.x = v.x + dx;
+      r.y = v.y + dy;
       out[o] = r;
     }
   }
@@ -395,24 +406,25 @@ __global__ void lawson_stage_kernel(int s, const cplx<R>* V, const cplx<R>* n, c
 //   s = 4: mu = h/6 L;  s = 3: mu = h/3 E(h/2) L + h E(h/2) gp;  s = 2: mu = h/3 E(h/2) L + h/2 gp;
 //   s = 1: mu = h/6 E(h) L + h/2 E(h/2) gp   (L = adjoint of the step output, gp = previous stage adjoint)
 template <typename R>
-__global__ void adj_mu_kernel(int s, const cplx<R>* L, const cplx<R>* gp, cplx<R>* mu, Geo g, double nu, double h) {
+__global__ void adj_mu_kernel(int s, const cplx<R>* L, const cplx<R>* gp, cplx<R>* mu, Geo g, double nu, double hd) {
   ModeIdx m;
+  const R h = R(hd);
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; mode_of(idx, g, m);
        idx += (long long)gridDim.x * blockDim.x) {
-    const double lin = nu * m.k2;
-    const double e1 = exp(-lin * h), eh = exp(-0.5 * lin * h);
-    double cl, cg;
-    if (s == 4) { cl = h / 6.0; cg = 0.0; }
-    else if (s == 3) { cl = h / 3.0 * eh; cg = h * eh; }
-    else if (s == 2) { cl = h / 3.0 * eh; cg = 0.5 * h; }
-    else { cl = h / 6.0 * e1; cg = 0.5 * h * eh; }
+    const R lin = R(nu * m.k2);
+    const R e1 = R(1) + wexpm1<R>(-lin * h), eh = R(1) + wexpm1<R>(R(-0.5) * lin * h);
+    R cl, cg;
+    if (s == 4) { cl = h / R(6); cg = R(0); }
+    else if (s == 3) { cl = h / R(3) * eh; cg = h * eh; }
+    else if (s == 2) { cl = h / R(3) * eh; cg = R(0.5) * h; }
+    else { cl = h / R(6) * e1; cg = R(0.5) * h * eh; }
+#pragma unroll
     for (int f = 0; f < 3; ++f) {
       const long long o = f * g.sS + m.o;
-      double x = cl * double(L[o].x), y = cl * double(L[o].y);
-      if (s != 4) { x += cg * double(gp[o].x); y += cg * double(gp[o].y); }
       cplx<R> r;
-      r.x = R(x);
-      r.y = R(y);
+      r.x = cl * L[o].x;
+      r.y = cl * L[o].y;
+      if (s != 4) { r.x += cg * gp[o].x; r.y += cg * gp[o].y; }
       mu[o] = r;
     }
   }
@@ -422,17 +434,19 @@ __global__ void adj_mu_kernel(int s, const cplx<R>* L, const cplx<R>* gp, cplx<R
 //   lam = E(h) L + E(h/2) (g2 + g3) + E(h) g4 + g1
 template <typename R>
 __global__ void adj_lambda_kernel(const cplx<R>* L, const cplx<R>* g1, const cplx<R>* g2, const cplx<R>* g3,
-                                  const cplx<R>* g4, cplx<R>* lam, Geo g, double nu, double h) {
+                                  const cplx<R>* g4, cplx<R>* lam, Geo g, double nu, double hd) {
   ModeIdx m;
+  const R h = R(hd);
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; mode_of(idx, g, m);
        idx += (long long)gridDim.x * blockDim.x) {
-    const double lin = nu * m.k2;
-    const double e1 = exp(-lin * h), eh = exp(-0.5 * lin * h);
+    const R lin = R(nu * m.k2);
+    const R e1 = R(1) + wexpm1<R>(-lin * h), eh = R(1) + wexpm1<R>(R(-0.5) * lin * h);
+#pragma unroll
     for (int f = 0; f < 3; ++f) {
       const long long o = f * g.sS + m.o;
       cplx<R> r;
-      r.x = R(e1 * (double(L[o].x) + double(g4[o].x)) + eh * (double(g2[o].x) + double(g3[o].x)) + double(g1[o].x));
-      r.y = R(e1 * (double(L[o].y) + double(g4[o].y)) + eh * (double(g2[o].y) + double(g3[o].y)) + double(g1[o].y));
+      r.x = e1 * (L[o].x + g4[o].x) + eh * (g2[o].x + g3[o].x) + g1[o].x;
+      r.y = e1 * (L[o].y + g4[o].y) + eh * (g2[o].y + g3[o].y) + g1[o].y;
       lam[o] = r;
     }
   }
@@ -446,31 +460,37 @@ __global__ void __launch_bounds__(kDiagThreads) adj_dnu_partial(const cplx<R>* L
                                                                 const cplx<R>* a2, const cplx<R>* n1,
                                                                 const cplx<R>* n2, const cplx<R>* n3,
                                                                 const cplx<R>* g2, const cplx<R>* g3,
-                                                                const cplx<R>* g4, Geo g, double nu, double h,
+                                                                const cplx<R>* g4, Geo g, double nu, double hd,
                                                                 double* part) {
-  Neumaier q;
+  // per mode in working precision, accumulated in FP64 (plain sum per thread, fixed tree per block)
+  double acc_t = 0.0;
   ModeIdx m;
+  const R h = R(hd);
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; mode_of(idx, g, m);
        idx += (long long)gridDim.x * blockDim.x) {
-    const double lin = nu * m.k2;
-    const double e1 = exp(-lin * h), eh = exp(-0.5 * lin * h);
-    const double kk = m.k2;
-    double acc = 0.0;
+    const R kk = R(m.k2);
+    const R lin = R(nu) * kk;
+    const R e1 = R(1) + wexpm1<R>(-lin * h), eh = R(1) + wexpm1<R>(R(-0.5) * lin * h);
+    R acc = R(0);
+#pragma unroll
     for (int f = 0; f < 3; ++f) {
       const long long o = f * g.sS + m.o;
-      auto dot = [&](const cplx<R>* A, double bx, double by) { return double(A[o].x) * bx + double(A[o].y) * by; };
-      const double vx = V[o].x, vy = V[o].y;
-      acc += dot(g2, -kk * 0.5 * h * double(a2[o].x), -kk * 0.5 * h * double(a2[o].y));
-      acc += dot(g3, -kk * 0.5 * h * eh * vx, -kk * 0.5 * h * eh * vy);
-      acc += dot(g4, -kk * h * e1 * vx - kk * 0.5 * h * h * eh * double(n3[o].x),
-                 -kk * h * e1 * vy - kk * 0.5 * h * h * eh * double(n3[o].y));
-      acc += dot(L, -kk * h * e1 * vx - kk * h * h / 6.0 * (e1 * double(n1[o].x) + eh * (double(n2[o].x) + double(n3[o].x))),
-                 -kk * h * e1 * vy - kk * h * h / 6.0 * (e1 * double(n1[o].y) + eh * (double(n2[o].y) + double(n3[o].y))));
+      const cplx<R> v = V[o], x2 = a2[o], y1 = n1[o], y2 = n2[o], y3 = n3[o];
+      const cplx<R> G2 = g2[o], G3 = g3[o], G4 = g4[o], LL = L[o];
+      const R c2 = -kk * R(0.5) * h, c3 = -kk * R(0.5) * h * eh;
+      acc += G2.x * c2 * x2.x + G2.y * c2 * x2.y;
+      acc += G3.x * c3 * v.x + G3.y * c3 * v.y;
+      const R b4x = -kk * h * e1 * v.x - kk * R(0.5) * h * h * eh * y3.x;
+      const R b4y = -kk * h * e1 * v.y - kk * R(0.5) * h * h * eh * y3.y;
+      acc += G4.x * b4x + G4.y * b4y;
+      const R bLx = -kk * h * e1 * v.x - kk * h * h / R(6) * (e1 * y1.x + eh * (y2.x + y3.x));
+      const R bLy = -kk * h * e1 * v.y - kk * h * h / R(6) * (e1 * y1.y + eh * (y2.y + y3.y));
+      acc += LL.x * bLx + LL.y * bLy;
     }
-    q.add(m.w * acc);
+    acc_t += m.w * double(acc);
   }
   __shared__ double sh[kDiagThreads];
-  sh[threadIdx.x] = q.value();
+  sh[threadIdx.x] = acc_t;
   __syncthreads();
   for (int s = kDiagThreads / 2; s > 0; s >>= 1) {
     if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
@@ -479,13 +499,13 @@ __global__ void __launch_bounds__(kDiagThreads) adj_dnu_partial(const cplx<R>* L
   if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
-// acc += fixed-order compensated sum of nblk partials (single thread)
+// acc += fixed-order sum of nblk partials (one warp: strided lane sums, then a fixed
+// shuffle tree, so the result does not depend on scheduling)
 __global__ void accumulate_partials(const double* part, int nblk, double* acc) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    Neumaier s;
-    for (int b = 0; b < nblk; ++b) s.add(part[b]);
-    *acc += s.value();
-  }
+  double v = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += 32) v += part[b];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (threadIdx.x == 0) *acc += v;
 }
 
 // gradient of the enstrophy 0.5 sum_half w |k x V|^2:  lam = k^2 V - k (k . V)
@@ -1283,7 +1303,9 @@ struct Adjoint {
   C *g1 = nullptr, *g2 = nullptr, *g3 = nullptr, *g4 = nullptr;
   C *seg = nullptr, *ck = nullptr;
   double* dnu = nullptr;
+  double* dpart = nullptr;  // per-block partial sums of d(loss)/d(nu)
   int blocks = 0;
+  static constexpr int kDnuBlocks = 1024;
 
   ~Adjoint() {
     for (void* b : bufs) cudaFree(b);
@@ -1308,7 +1330,8 @@ struct Adjoint {
         {(void**)&n1, fbytes}, {(void**)&n2, fbytes}, {(void**)&n3, fbytes}, {(void**)&a2, fbytes},
         {(void**)&a3, fbytes}, {(void**)&a4, fbytes}, {(void**)&g1, fbytes}, {(void**)&g2, fbytes},
         {(void**)&g3, fbytes}, {(void**)&g4, fbytes}, {(void**)&seg, fbytes * (size_t)seglen},
-        {(void**)&ck, fbytes * (size_t)nck}, {(void**)&dnu, sizeof(double)}};
+        {(void**)&ck, fbytes * (size_t)nck}, {(void**)&dnu, sizeof(double)},
+        {(void**)&dpart, sizeof(double) * kDnuBlocks}};
     for (auto& b : list)
       if ((rc = alloc(b.ptr, b.bytes))) return rc;
     const long long modes = (long long)g.M * g.M * g.Hk;
@@ -1337,12 +1360,44 @@ struct Adjoint {
     a.spec_out = out;
     a.spec_in = X;
     a.nin = 3;
+    if (sizeof(R) == 4 && has_reg_adjoint(p->n) && p->variant == 0)
+      return Ops<R>::go(p, OP_KX_NL_FWD, a, "kx nonlinear");
     a.flags |= FLAG_NONLIN;
     return Ops<R>::go(p, OP_KX_FWD3, a, "kx nonlinear");
   }
   // out = N'(W)^T mu = F[omega x a] + i k x F[a x u],  a = F^-1 (P mu), (u, omega) of W
   int nonlin_adj(const C* W, const C* m, C* out) {
     int rc;
+    if (sizeof(R) == 4 && has_reg_adjoint(p->n) && p->variant == 0) {
+      PassArgs<R> a = Ops<R>::base(p);
+      a.spec_in = W;
+      a.S = const_cast<C*>(m);
+      a.out = X9;
+      a.nin = 6;
+      a.nout = 9;
+      if ((rc = Ops<R>::go(p, OP_KX_ADJ_LOAD, a, "kx adjoint load"))) return rc;
+      a = Ops<R>::base(p);
+      a.in = X9;
+      a.out = Y9;
+      a.nin = a.nout = 9;
+      if ((rc = Ops<R>::go(p, OP_KY_INV, a, "ky adjoint inverse"))) return rc;
+      a = Ops<R>::base(p);
+      a.in = Y9;
+      a.out = Z6;
+      a.nin = 9;
+      a.nout = 6;
+      if ((rc = Ops<R>::go(p, OP_KZ_ADJ, a, "kz adjoint"))) return rc;
+      a = Ops<R>::base(p);
+      a.in = Z6;
+      a.out = Y9;
+      a.nin = a.nout = 6;
+      if ((rc = Ops<R>::go(p, OP_KY_FWD, a, "ky adjoint forward"))) return rc;
+      a = Ops<R>::base(p);
+      a.in = Y9;
+      a.spec_out = out;
+      a.nin = 6;
+      return Ops<R>::go(p, OP_KX_ADJ_FWD, a, "kx adjoint forward");
+    }
     if ((rc = copy(WMU, W))) return rc;
     if ((rc = copy(WMU + 3 * p->g.sS, m))) return rc;
     PassArgs<R> a = Ops<R>::base(p);
@@ -1401,8 +1456,8 @@ struct Adjoint {
     adj_mu_kernel<R><<<blocks, 256, 0, st>>>(1, L, g2, mu, g, nu, h);
     if ((rc = nonlin_adj(V, mu, g1))) return rc;
     adj_lambda_kernel<R><<<blocks, 256, 0, st>>>(L, g1, g2, g3, g4, lam_out, g, nu, h);
-    adj_dnu_partial<R><<<kDiagBlocks, kDiagThreads, 0, st>>>(L, V, a2, n1, n2, n3, g2, g3, g4, g, nu, h, p->part);
-    accumulate_partials<<<1, 32, 0, st>>>(p->part, kDiagBlocks, dnu);
+    adj_dnu_partial<R><<<kDnuBlocks, kDiagThreads, 0, st>>>(L, V, a2, n1, n2, n3, g2, g3, g4, g, nu, h, dpart);
+    accumulate_partials<<<1, 32, 0, st>>>(dpart, kDnuBlocks, dnu);
     p->launches += 10;
     return launch_check("adjoint combine");
   }
@@ -1419,8 +1474,8 @@ struct Adjoint {
     for (int c = 0; c < nck; ++c) {
       if ((rc = copy(ck + (size_t)c * 3 * g.sS, cur))) return rc;
       const int len = std::min(seglen, nsteps - c * seglen);
-      for (int j = 0; j < len; ++j)
-        if ((rc = step(cur))) return rc;
+      if ((rc = Ops<R>::start(p, cur))) return rc;
+      if ((rc = advance(p, cur, len))) return rc;  // graph-launched steps
     }
     // loss = enstrophy of the final state, and its gradient
     if ((rc = Ops<R>::diagnostics(p, cur, p->dtmp))) return rc;

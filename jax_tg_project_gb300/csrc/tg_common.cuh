@@ -75,7 +75,7 @@ template <typename R, int N, int BUFS = 7> struct LinesZ {
   static constexpr int value = fit(pref);
 };
 
-enum KxMode { KX_STAGE = 0, KX_LOAD = 1, KX_FWD = 2 };
+enum KxMode { KX_STAGE = 0, KX_LOAD = 1, KX_FWD = 2, KX_ADJ_LOAD = 3, KX_ADJ_FWD = 4, KX_NL_FWD = 5 };
 enum FieldMap { MAP_ID = 0, MAP_UW = 1, MAP_UWBJ = 2, MAP_DIV = 3, MAP_DIVB = 4, MAP_CURL = 5, MAP_ADJ = 6 };
 enum KzMode { KZ_PROD_HD = 0, KZ_PROD_MHD = 1, KZ_C2R = 2, KZ_R2C = 3, KZ_ADJ = 4 };
 enum Flags { FLAG_EXPLICIT = 1, FLAG_RHS = 2, FLAG_AMAX = 4, FLAG_NONLIN = 8, FLAG_ADJ = 16 };

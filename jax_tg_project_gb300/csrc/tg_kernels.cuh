@@ -583,7 +583,8 @@ kz_kernel(const PassArgs<R> a) {
 // ------------------------------------------------------------------ launcher
 enum PassOp {
   OP_KX_STAGE3 = 0, OP_KX_STAGE6, OP_KX_LOAD3, OP_KX_LOAD6, OP_KX_FWD3, OP_KX_FWD6,
-  OP_KY_INV, OP_KY_FWD, OP_KZ_PROD_HD, OP_KZ_PROD_MHD, OP_KZ_C2R, OP_KZ_R2C, OP_KZ_ADJ, OP_COUNT
+  OP_KY_INV, OP_KY_FWD, OP_KZ_PROD_HD, OP_KZ_PROD_MHD, OP_KZ_C2R, OP_KZ_R2C, OP_KZ_ADJ,
+  OP_KX_ADJ_LOAD, OP_KX_ADJ_FWD, OP_KX_NL_FWD, OP_COUNT  // the last three: register-resident only
 };
 
 template <typename K>

@@ -387,6 +387,142 @@ static cudaError_t launch_kz_reg_mhd(const PassArgs<R>& a, int runs, cudaStream_
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ z pass, adjoint
+// Adjoint of u x omega for one line pair: inverse transforms of u, omega (state) and
+// a (projected adjoint field); outputs p = omega x a (fields 0..2) and q = a x u (3..5).
+// Order: a, u -> registers; q transformed straight from them; omega accumulates p.
+template <typename R, int N>
+__global__ void __launch_bounds__(128) kz_reg_adj_kernel(const PassArgs<R> a) {
+  using C = cplx<R>;
+  using Sh = KzRegMhdShape<R, N>;  // same footprint: 9 staged fields per pair
+  using Plan = typename Sh::Plan;
+  constexpr int P = Sh::P, E = Sh::E, LP = Sh::LP, CS = Sh::CS;
+  constexpr int NBL = N / (Plan::template radix<Plan::NPASS - 1>() * P);
+  const Geo g = a.g;
+  const int K = g.K, Hz = g.Hz;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  const int t = threadIdx.x % P, lp = threadIdx.x / P;
+  C* xcol = tw + N + lp * Sh::per_pair;
+  C* stg = xcol + CS;  // slot i at stg + i * SS
+  const int pair = blockIdx.x * LP + lp, run = blockIdx.y;
+  const int x = pair / (N / 2), y0 = 2 * (pair % (N / 2));
+  const long long row0 = ((long long)x * N + y0) * Hz;
+  const C* yin = a.in + (long long)run * 9 * g.sY;
+  C* zout = a.out + (long long)run * 6 * g.sY;
+  // slots in order of use: a (fields 6,7,8), u (0,1,2), omega (3,4,5)
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    const int f = (i < 3) ? i + 6 : ((i < 6) ? i - 3 : i - 3);
+    const C* src = yin + f * g.sY + row0;
+    C* dst = stg + i * Sh::SS;
+    for (int c = t; c < Hz; c += P) cp_async16(dst + 2 * c, src + 2 * c);
+    cp_async_commit();
+  }
+  build_twiddles<Plan>(tw, a.tw, threadIdx.x, Sh::NT);
+  __syncthreads();
+  const WarpSync ws;
+  auto packed = [&](const C* fld) {
+    return [=](int k, int) -> C {
+      if (k <= K) {
+        C A = fld[k], B = fld[Hz + k];
+        if (k == 0) { A.y = 0; B.y = 0; }
+        return mk<C>(A.x - B.y, A.y + B.x);
+      }
+      if (k >= N - K) {
+        const C A = fld[N - k], B = fld[Hz + (N - k)];
+        return mk<C>(A.x + B.y, B.x - A.y);
+      }
+      return czero<C>();
+    };
+  };
+  C z[E];
+  auto forward_store = [&](auto& src, int c) {
+    auto dst = [&](int b, int r, int, C v) { z[b + r * NBL] = v; };
+    fft_column<Plan, -1, Sh::PSH>(t, src, dst, xcol, tw, ws);
+    C zm[E];
+    const int src_lane = (P - t) % P;
+#pragma unroll
+    for (int qq = 0; qq < E; ++qq) {
+      C v;
+      v.x = __shfl_sync(0xffffffffu, z[qq].x, src_lane, P);
+      v.y = __shfl_sync(0xffffffffu, z[qq].y, src_lane, P);
+      zm[E - 1 - qq] = (t != 0) ? v : z[(qq + 1) % E];
+    }
+    C* outf = zout + c * g.sY + row0;
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      const int k = t + P * q;
+      if (k <= K) {
+        outf[k] = mk<C>((z[q].x + zm[q].x) * R(0.5), (z[q].y - zm[q].y) * R(0.5));
+        outf[Hz + k] = mk<C>((z[q].y + zm[q].y) * R(0.5), (zm[q].x - z[q].x) * R(0.5));
+      }
+    }
+  };
+  C av[3][E], u[3][E];
+  auto inv_to = [&](auto slot_tag, auto wait_tag, auto* dstarr) {
+    constexpr int SLOT = decltype(slot_tag)::value;
+    cp_async_wait<decltype(wait_tag)::value>();
+    __syncwarp();
+    auto src = packed(stg + SLOT * Sh::SS);
+    auto dst = [&](int bb, int r, int, C v) { dstarr[bb + r * NBL] = v; };
+    fft_column<Plan, +1, Sh::PSH>(t, src, dst, xcol, tw, ws);
+  };
+  inv_to(std::integral_constant<int, 0>(), std::integral_constant<int, 8>(), av[0]);
+  inv_to(std::integral_constant<int, 1>(), std::integral_constant<int, 7>(), av[1]);
+  inv_to(std::integral_constant<int, 2>(), std::integral_constant<int, 6>(), av[2]);
+  inv_to(std::integral_constant<int, 3>(), std::integral_constant<int, 5>(), u[0]);
+  inv_to(std::integral_constant<int, 4>(), std::integral_constant<int, 4>(), u[1]);
+  inv_to(std::integral_constant<int, 5>(), std::integral_constant<int, 3>(), u[2]);
+  {  // q = a x u -> fields 3..5
+    auto q0 = [&](int, int q) -> C { return mk<C>(av[1][q].x * u[2][q].x - av[2][q].x * u[1][q].x,
+                                                  av[1][q].y * u[2][q].y - av[2][q].y * u[1][q].y); };
+    auto q1 = [&](int, int q) -> C { return mk<C>(av[2][q].x * u[0][q].x - av[0][q].x * u[2][q].x,
+                                                  av[2][q].y * u[0][q].y - av[0][q].y * u[2][q].y); };
+    auto q2 = [&](int, int q) -> C { return mk<C>(av[0][q].x * u[1][q].x - av[1][q].x * u[0][q].x,
+                                                  av[0][q].y * u[1][q].y - av[1][q].y * u[0][q].y); };
+    forward_store(q0, 3);
+    forward_store(q1, 4);
+    forward_store(q2, 5);
+  }
+  // p = omega x a:  (omega x a)_{w+1} -= omega_w a_{w+2};  (omega x a)_{w+2} += omega_w a_{w+1}
+  C pm[3][E];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int q = 0; q < E; ++q) pm[c][q] = czero<C>();
+  auto add_w = [&](auto w_tag, auto wait_tag) {
+    constexpr int w = decltype(w_tag)::value;
+    inv_to(std::integral_constant<int, 6 + w>(), wait_tag, z);
+    constexpr int c1 = (w + 1) % 3, c2 = (w + 2) % 3;
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      pm[c1][q] = mk<C>(pm[c1][q].x - z[q].x * av[c2][q].x, pm[c1][q].y - z[q].y * av[c2][q].y);
+      pm[c2][q] = mk<C>(pm[c2][q].x + z[q].x * av[c1][q].x, pm[c2][q].y + z[q].y * av[c1][q].y);
+    }
+  };
+  add_w(std::integral_constant<int, 0>(), std::integral_constant<int, 2>());
+  add_w(std::integral_constant<int, 1>(), std::integral_constant<int, 1>());
+  add_w(std::integral_constant<int, 2>(), std::integral_constant<int, 0>());
+  auto p0 = [&](int, int q) -> C { return pm[0][q]; };
+  auto p1 = [&](int, int q) -> C { return pm[1][q]; };
+  auto p2 = [&](int, int q) -> C { return pm[2][q]; };
+  forward_store(p0, 0);
+  forward_store(p1, 1);
+  forward_store(p2, 2);
+}
+
+template <typename R, int N>
+static cudaError_t launch_kz_reg_adj(const PassArgs<R>& a, int runs, cudaStream_t st) {
+  using Sh = KzRegMhdShape<R, N>;
+  static cudaError_t attr = set_smem(kz_reg_adj_kernel<R, N>, Sh::smem);
+  if (attr != cudaSuccess) return attr;
+  const int pairs = N * N / 2;
+  dim3 grid(pairs / Sh::LP, runs);
+  kz_reg_adj_kernel<R, N><<<grid, Sh::NT, Sh::smem, st>>>(a);
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ x pass
 template <typename R, int N>
 struct KxRegShape {
@@ -555,6 +691,159 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT) kx_reg_kernel(const Pass
   inverse(std::integral_constant<int, 3>());
   inverse(std::integral_constant<int, 4>());
   inverse(std::integral_constant<int, 5>());
+}
+
+// ------------------------------------------------------------------ x pass, adjoint
+// KX_ADJ_LOAD: inverse-x of u, curl u of the state W (spec_in) and of a = P mu (mu in S)
+//              -> 9 fields (u 0..2, omega 3..5, a 6..8)
+// KX_ADJ_FWD:  forward-x of p (0..2), q (3..5) -> spec_out = F p + i k x F q (1/N^3 applied)
+template <typename R, int N, int MODE>
+__global__ void __launch_bounds__(KxRegShape<R, N>::NT) kx_reg_adj_kernel(const PassArgs<R> a) {
+  using C = cplx<R>;
+  using Sh = KxRegShape<R, N>;
+  using Plan = typename Sh::Plan;
+  constexpr int P = Sh::P, E = Sh::E, QW = Sh::QW, GT = Sh::GT, CS = Sh::CS;
+  constexpr int NBL = N / (Plan::template radix<Plan::NPASS - 1>() * P);
+  const Geo g = a.g;
+  const int K = g.K, M = g.M, Hz = g.Hz;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  const int grp = threadIdx.x / GT, lt = threadIdx.x % GT;
+  const int col = lt % QW, t = lt / QW;
+  const int iyc = blockIdx.x, run = blockIdx.z;
+  const int kz = (blockIdx.y * Sh::NG + grp) * QW + col;
+  const bool zok = kz < g.Hk;
+  C* xcol = tw + N + (grp * QW + col) * CS;
+  build_twiddles<Plan>(tw, a.tw, threadIdx.x, Sh::NT);
+  __syncthreads();
+  const float kyf = float(ksigned(iyc, K)), kzf = float(kz);
+  const long long soff = (long long)run * 3 * g.sS + (long long)iyc * Hz + kz;
+  auto run_fft = [&](auto& src, auto& dst, auto dir_tag) {
+    constexpr int DIR = decltype(dir_tag)::value;
+    if constexpr (GT > 32) {
+      const NamedSync ns{1 + grp, GT};
+      fft_column<Plan, DIR, Sh::PSH>(t, src, dst, xcol, tw, ns);
+    } else {
+      const WarpSync ws;
+      fft_column<Plan, DIR, Sh::PSH>(t, src, dst, xcol, tw, ws);
+    }
+  };
+  using Fwd = std::integral_constant<int, -1>;
+  using Inv = std::integral_constant<int, +1>;
+  if constexpr (MODE == KX_ADJ_LOAD) {
+    C v[3][E], w[3][E];
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      const int ic = kcompact(t + P * q, N, K);
+      const bool ok = zok && ic >= 0;
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        const long long o = soff + ((long long)f * M + (ok ? ic : 0)) * M * Hz;
+        v[f][q] = ok ? a.spec_in[o] : czero<C>();
+        w[f][q] = ok ? a.S[o] : czero<C>();
+      }
+      if (ok) {
+        const float kx = float(ksigned(ic, K));
+        leray(w[0][q], w[1][q], w[2][q], kx, kyf, kzf, kx * kx + kyf * kyf + kzf * kzf);
+      }
+    }
+    C* xo = a.out + (long long)run * 9 * g.sX + (long long)iyc * Hz + kz;
+    auto inverse = [&](auto gi_tag) {
+      constexpr int GI = decltype(gi_tag)::value;
+      auto src = [&](int k, int q) -> C {
+        const int ic = kcompact(k, N, K);
+        if (ic < 0) return czero<C>();
+        if constexpr (GI < 6) return uw_field<GI>(v, q, float(ksigned(ic, K)), kyf, kzf);
+        else return w[GI - 6][q];
+      };
+      C* xg = xo + GI * g.sX;
+      auto dst = [&](int, int, int xx, C val) {
+        if (zok) xg[(long long)xx * M * Hz] = val;
+      };
+      run_fft(src, dst, Inv());
+    };
+    inverse(std::integral_constant<int, 0>());
+    inverse(std::integral_constant<int, 1>());
+    inverse(std::integral_constant<int, 2>());
+    inverse(std::integral_constant<int, 3>());
+    inverse(std::integral_constant<int, 4>());
+    inverse(std::integral_constant<int, 5>());
+    inverse(std::integral_constant<int, 6>());
+    inverse(std::integral_constant<int, 7>());
+    inverse(std::integral_constant<int, 8>());
+  } else if constexpr (MODE == KX_NL_FWD) {  // spec_out = P F(u x omega) / N^3 (nonlinear term alone)
+    const R inv_n3 = R(1) / (R(N) * R(N) * R(N));
+    const C* win = a.in + (long long)run * 3 * g.sX + (long long)iyc * Hz + kz;
+    C nv[3][E];
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      const C* wf = win + f * g.sX;
+      auto src = [&](int xx, int) -> C { return zok ? wf[(long long)xx * M * Hz] : czero<C>(); };
+      auto dst = [&](int b, int r, int, C val) { nv[f][b + r * NBL] = cscale(val, inv_n3); };
+      run_fft(src, dst, Fwd());
+    }
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      const int ic = kcompact(t + P * q, N, K);
+      if (zok && ic >= 0) {
+        const float kx = float(ksigned(ic, K));
+        leray(nv[0][q], nv[1][q], nv[2][q], kx, kyf, kzf, kx * kx + kyf * kyf + kzf * kzf);
+#pragma unroll
+        for (int f = 0; f < 3; ++f) a.spec_out[soff + ((long long)f * M + ic) * M * Hz] = nv[f][q];
+      }
+    }
+  } else {  // KX_ADJ_FWD
+    const R inv_n3 = R(1) / (R(N) * R(N) * R(N));
+    const C* win = a.in + (long long)run * 6 * g.sX + (long long)iyc * Hz + kz;
+    C acc[3][E], z[E];
+    auto fwd_to = [&](int f, auto* dstarr) {
+      const C* wf = win + f * g.sX;
+      auto src = [&](int xx, int) -> C { return zok ? wf[(long long)xx * M * Hz] : czero<C>(); };
+      auto dst = [&](int b, int r, int, C val) { dstarr[b + r * NBL] = cscale(val, inv_n3); };
+      run_fft(src, dst, Fwd());
+    };
+    fwd_to(0, acc[0]);
+    fwd_to(1, acc[1]);
+    fwd_to(2, acc[2]);
+    // + i k x F q, one component of q at a time
+    auto add_curl = [&](auto c_tag) {
+      constexpr int c = decltype(c_tag)::value;
+      fwd_to(3 + c, z);
+#pragma unroll
+      for (int q = 0; q < E; ++q) {
+        const int ic = kcompact(t + P * q, N, K);
+        const float kx = float(ksigned(ic < 0 ? 0 : ic, K));
+        const float kk[3] = {kx, kyf, kzf};
+        // (k x e_c q)_{c+1} = k_{c+2} q,  (k x e_c q)_{c+2} = -k_{c+1} q; then times i
+        constexpr int c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+        const C iz = cmul_i(z[q]);
+        acc[c1][q] = mk<C>(acc[c1][q].x + R(kk[c2]) * iz.x, acc[c1][q].y + R(kk[c2]) * iz.y);
+        acc[c2][q] = mk<C>(acc[c2][q].x - R(kk[c1]) * iz.x, acc[c2][q].y - R(kk[c1]) * iz.y);
+      }
+    };
+    add_curl(std::integral_constant<int, 0>());
+    add_curl(std::integral_constant<int, 1>());
+    add_curl(std::integral_constant<int, 2>());
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      const int ic = kcompact(t + P * q, N, K);
+      if (zok && ic >= 0) {
+#pragma unroll
+        for (int f = 0; f < 3; ++f) a.spec_out[soff + ((long long)f * M + ic) * M * Hz] = acc[f][q];
+      }
+    }
+  }
+}
+
+template <typename R, int N, int MODE>
+static cudaError_t launch_kx_reg_adj(const PassArgs<R>& a, int runs, cudaStream_t st) {
+  using Sh = KxRegShape<R, N>;
+  static cudaError_t attr = set_smem(kx_reg_adj_kernel<R, N, MODE>, Sh::smem);
+  if (attr != cudaSuccess) return attr;
+  const int quads = (a.g.Hk + Sh::QW - 1) / Sh::QW;
+  dim3 grid(a.g.M, (quads + Sh::NG - 1) / Sh::NG, runs);
+  kx_reg_adj_kernel<R, N, MODE><<<grid, Sh::NT, Sh::smem, st>>>(a);
+  return cudaGetLastError();
 }
 
 template <typename R, int N>
