@@ -136,7 +136,9 @@ int tg_step(tg_plan* plan, void* state, double dt, double nu, double eta, int ns
 /* The run loop (jax/taylor_green_jax.py:266-275, cuda/taylor_green_mhd/simulation.py:59-68):
  * records diagnostics of the initial state, then after every save_every steps
  * and after the last step.  series (device) receives [records][batch][TG_DIAG_WIDTH]
- * doubles with records = 1 + nsteps/save_every + (nsteps % save_every != 0). */
+ * doubles with records = 1 + nsteps/save_every + (nsteps % save_every != 0).
+ * Synchronises at the end and returns TG_E_NONFINITE if any recorded value is NaN/Inf
+ * (the series is still written; the message names the first bad record). */
 int tg_run(tg_plan* plan, void* state, double dt, double nu, double eta, int nsteps,
            int save_every, double* series);
 

@@ -1203,6 +1203,17 @@ int tg_run(tg_plan* p, void* state, double dt, double nu, double eta, int nsteps
     ++rec;
   }
   p->launches = total;
+  // failure detection: a non-finite diagnostic means the run blew up (e.g. dt above the
+  // stability limit, or a NaN in the initial state); report the first such record
+  std::vector<double> h((size_t)rec * stride);
+  TG_CUDA(cudaMemcpyAsync(h.data(), series, h.size() * sizeof(double), cudaMemcpyDeviceToHost, p->st),
+          "series readback");
+  TG_CUDA(cudaStreamSynchronize(p->st), "tg_run sync");
+  for (int r = 0; r < rec; ++r)
+    for (long long i = 0; i < stride; ++i)
+      if (!std::isfinite(h[(size_t)r * stride + i]))
+        return fail(TG_E_NONFINITE, "tg_run: non-finite diagnostics at record " + std::to_string(r) +
+                                        " (run " + std::to_string(i / TG_DIAG_WIDTH) + ")");
   return TG_OK;
 }
 

@@ -143,3 +143,22 @@ def test_fp32_step_tracks_fp64_gpu_run_at_256():
     b = from_state(p64, s64)[0]
     assert rel_l2(a, b) < 1e-5
     del p32, p64
+
+
+def test_run_reports_non_finite_state():
+    """Failure detection without a GPU fault: a NaN placed in a host-built state makes
+    tg_run return TG_E_NONFINITE, and the plan keeps working afterwards."""
+    import torch
+
+    from jax_tg_project_gb300 import _abi
+    p = _plan(16, "f32")
+    s = p.initial_condition("taylor_green")
+    host = s.cpu()
+    host[0, 0, 1, 1, 1] = complex(float("nan"), 0.0)
+    bad = host.to(p.device)
+    with pytest.raises(_abi.TgError) as e:
+        p.run(bad, dt=0.005, nu=0.01, nsteps=4, save_every=2)
+    assert e.value.code == _abi.TG_E_NONFINITE and "record 0" in str(e.value)
+    good = p.initial_condition("taylor_green")
+    series = p.run(good, dt=0.005, nu=0.01, nsteps=4, save_every=2)
+    assert torch.isfinite(series).all()
