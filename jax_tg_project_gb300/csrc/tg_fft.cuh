@@ -129,13 +129,25 @@ struct FftPlan {
   static constexpr int E = N_ / P_;  // elements held per thread per pass
 };
 
-// padded shared-memory index: one spare slot every 2^PSH complex values
+// Exchange-buffer index.  PSH >= 0: one spare slot every 2^PSH complex values.
+// PSH == kSwizzle: no spare slots; the low four index bits (the 16 eight-byte
+// bank pairs) are XORed with (n4, n5, n6, n4 ^ n5).  For the register plans
+// (8,2,8) / (8,4,8) with P = 16 / 32 threads per transform (N = 128 / 256) every
+// exchange store and load of a half warp then touches 16 distinct bank pairs.
+constexpr int kSwizzle = -1;
 template <int PSH = 4>
-__device__ __forceinline__ int padx(int n) { return n + (n >> PSH); }
+__device__ __forceinline__ int padx(int n) {
+  if constexpr (PSH == kSwizzle) {
+    const int h = n >> 4;
+    return n ^ ((h & 7) | (((h ^ (h >> 1)) & 1) << 3));
+  } else {
+    return n + (n >> PSH);
+  }
+}
 // per-column stride in complex elements, congruent to CSMOD modulo 16 (the 16
 // eight-byte bank pairs), so that the columns of a CTA interleave banks
 template <int N, int PSH = 4, int CSMOD = 1> struct ColLayout {
-  static constexpr int PADN = N + (N >> PSH);
+  static constexpr int PADN = (PSH == kSwizzle) ? N : N + (N >> PSH);
   static constexpr int CS = PADN + (((CSMOD - PADN) % 16) + 16) % 16;
 };
 
@@ -156,6 +168,14 @@ __device__ __forceinline__ void build_twiddles(C* dst, const C* wn, int tid, int
     }
     build_twiddles<Plan, I + 1, NS * R>(dst, wn, tid, nthr);
   }
+}
+
+// j mod NS for j >= 0 (a mask for powers of two, so that jm of the butterflies
+// b and b + 1 of a thread is seen to be equal when P is a multiple of NS)
+template <int NS>
+__device__ __forceinline__ int jmod(int j) {
+  if constexpr ((NS & (NS - 1)) == 0) return j & (NS - 1);
+  else return j % NS;
 }
 
 // Barriers between passes: the threads that share exchange columns.
@@ -181,7 +201,8 @@ struct NamedSync {  // bar.sync on a named barrier shared by `count` threads (wh
 // Thread t reads exactly the inputs n = t (mod P) in pass 0 and holds exactly the
 // outputs k = t (mod P) after the last pass (q = b + r*N/(R*P) in both), so a
 // transform can take its input from, and leave its output in, registers.
-template <class Plan, int DIR, int I, int NS, int PSH = 4, typename C, class Src, class Dst, class Sync = CtaSync>
+template <class Plan, int DIR, int I, int NS, int PSH = 4, bool TWC = false, typename C, class Src, class Dst,
+          class Sync = CtaSync>
 __device__ __forceinline__ void fft_pass(int t, Src& src, Dst& dst, C* xb, const C* tw,
                                          const Sync& sync = Sync()) {
   constexpr int N = Plan::N, P = Plan::P;
@@ -201,13 +222,25 @@ __device__ __forceinline__ void fft_pass(int t, Src& src, Dst& dst, C* xb, const
       }
     }
     if constexpr (I > 0) {
-      const int jm = j % NS;
+      const int jm = jmod<NS>(j);
+      constexpr int OFF = NS - Plan::template radix<0>();
+      C w[R];
+      if constexpr (TWC && sizeof(w[0].x) == 4) {
+        // read W^jm only and form W^(jm r) = W^(jm r/2) W^(jm (r - r/2)) in registers
+        // (at most log2(R) products deep): fewer table reads on the shared-memory pipe
+        w[1] = tw[OFF + jm];
+        if constexpr (DIR > 0) w[1].y = -w[1].y;
 #pragma unroll
-      for (int r = 1; r < R; ++r) {
-        C w = tw[(NS - Plan::template radix<0>()) + (r - 1) * NS + jm];
-        if constexpr (DIR > 0) w.y = -w.y;
-        v[b][r] = cmul(v[b][r], w);
+        for (int r = 2; r < R; ++r) w[r] = cmul(w[r / 2], w[r - r / 2]);
+      } else {
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          w[r] = tw[OFF + (r - 1) * NS + jm];
+          if constexpr (DIR > 0) w[r].y = -w[r].y;
+        }
       }
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], w[r]);
     }
     dft<R, DIR>(v[b]);
   }
@@ -216,13 +249,13 @@ __device__ __forceinline__ void fft_pass(int t, Src& src, Dst& dst, C* xb, const
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
       const int j = t + P * b;
-      const int jm = j % NS;
-      const int base = (j / NS) * NS * R + jm;
+      const int jm = jmod<NS>(j);
+      const int base = (j - jm) * R + jm;
 #pragma unroll
       for (int r = 0; r < R; ++r) xb[padx<PSH>(base + r * NS)] = v[b][r];
     }
     sync();
-    fft_pass<Plan, DIR, I + 1, NS * R, PSH>(t, src, dst, xb, tw, sync);
+    fft_pass<Plan, DIR, I + 1, NS * R, PSH, TWC>(t, src, dst, xb, tw, sync);
   } else {
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
@@ -233,10 +266,10 @@ __device__ __forceinline__ void fft_pass(int t, Src& src, Dst& dst, C* xb, const
   }
 }
 
-template <class Plan, int DIR, int PSH = 4, typename C, class Src, class Dst, class Sync = CtaSync>
+template <class Plan, int DIR, int PSH = 4, bool TWC = false, typename C, class Src, class Dst, class Sync = CtaSync>
 __device__ __forceinline__ void fft_column(int t, Src& src, Dst& dst, C* xb, const C* tw,
                                            const Sync& sync = Sync()) {
-  fft_pass<Plan, DIR, 0, 1, PSH>(t, src, dst, xb, tw, sync);
+  fft_pass<Plan, DIR, 0, 1, PSH, TWC>(t, src, dst, xb, tw, sync);
 }
 
 // register slot q of the output (b, r) of the last pass

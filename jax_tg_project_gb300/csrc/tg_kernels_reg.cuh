@@ -16,7 +16,10 @@
 //
 // Shared memory holds only the twiddle table and one exchange column per
 // transform, so barriers are per warp (z) or per 4-column group (x, a named
-// barrier), never CTA-wide inside the loops.
+// barrier), never CTA-wide inside the loops.  The z passes at N >= 128 use the
+// XOR-swizzled exchange layout (no bank conflicts) and form the twiddle powers in
+// registers from one table read per butterfly; the x pass keeps the table (its
+// four columns share each twiddle, so a read is a broadcast).
 #pragma once
 
 #include <type_traits>
@@ -56,7 +59,8 @@ struct KzRegShape {
   static constexpr int P = Plan::P, E = Plan::E;
   static constexpr int NT = 128;
   static constexpr int LP = NT / P;  // line pairs per CTA
-  static constexpr int PSH = (N >= 64) ? 4 : 3;  // exchange padding (bank-conflict model, see DESIGN)
+  // exchange layout: XOR swizzle at N >= 128, padding below (bank-conflict model)
+  static constexpr int PSH = (N >= 128) ? kSwizzle : (N >= 64) ? 4 : 3;
   static constexpr int CS = ColLayout<N, PSH, (N == 16) ? 2 : 4>::CS;
   static constexpr int HZMAX = ((N / 3 + 1) + 3) / 4 * 4;
   // per pair: exchange column + the two spectral rows of the six input fields
@@ -127,7 +131,7 @@ __global__ void __launch_bounds__(128, 3) kz_reg_kernel(const PassArgs<R> a) {
     ready(c_tag);
     auto src = packed(stg + c * 2 * Hz);
     auto dst = [&](int b, int r, int, C v) { u[c][b + r * NBL] = v; };
-    fft_column<Plan, +1, Sh::PSH>(t, src, dst, xcol, tw, ws);
+    fft_column<Plan, +1, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
   };
   inv_u(std::integral_constant<int, 0>());
   inv_u(std::integral_constant<int, 1>());
@@ -142,7 +146,7 @@ __global__ void __launch_bounds__(128, 3) kz_reg_kernel(const PassArgs<R> a) {
     ready(std::integral_constant<int, 3 + w>());
     auto src = packed(stg + (3 + w) * 2 * Hz);
     auto dst = [&](int b, int r, int, C v) { z[b + r * NBL] = v; };
-    fft_column<Plan, +1, Sh::PSH>(t, src, dst, xcol, tw, ws);
+    fft_column<Plan, +1, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
     constexpr int c1 = (w + 1) % 3, c2 = (w + 2) % 3;
 #pragma unroll
     for (int q = 0; q < E; ++q) {
@@ -158,7 +162,7 @@ __global__ void __launch_bounds__(128, 3) kz_reg_kernel(const PassArgs<R> a) {
   for (int c = 0; c < 3; ++c) {
     auto src = [&](int, int q) -> C { return m[c][q]; };
     auto dst = [&](int b, int r, int, C v) { z[b + r * NBL] = v; };
-    fft_column<Plan, -1, Sh::PSH>(t, src, dst, xcol, tw, ws);
+    fft_column<Plan, -1, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
     // partner value Z(N-k) for k = t + P q: lane (P-t) mod P, slot E-1-q (t != 0) or
     // this lane, slot (E-q) mod E (t == 0)
     C zm[E];
@@ -194,7 +198,7 @@ struct KzRegMhdShape {
   static constexpr int P = Plan::P, E = Plan::E;
   static constexpr int NT = 128;
   static constexpr int LP = NT / P;
-  static constexpr int PSH = (N >= 64) ? 4 : 3;
+  static constexpr int PSH = (N >= 128) ? kSwizzle : (N >= 64) ? 4 : 3;
   static constexpr int CS = ColLayout<N, PSH, (N == 16) ? 2 : 4>::CS;
   static constexpr int HZMAX = ((N / 3 + 1) + 3) / 4 * 4;
   static constexpr int NSTAGE = 9;        // staging slots, in order of use: u (0..2), b (3..5), omega (6..8)
@@ -271,7 +275,7 @@ __global__ void __launch_bounds__(128) kz_reg_mhd_kernel(const PassArgs<R> a) {
   // forward transform of a register field given by src(q), Hermitian unpack, store field c
   auto forward_store = [&](auto& src, int c) {
     auto dst = [&](int b, int r, int, C v) { z[b + r * NBL] = v; };
-    fft_column<Plan, -1, Sh::PSH>(t, src, dst, xcol, tw, ws);
+    fft_column<Plan, -1, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
     C zm[E];
     const int src_lane = (P - t) % P;
 #pragma unroll
@@ -299,7 +303,7 @@ __global__ void __launch_bounds__(128) kz_reg_mhd_kernel(const PassArgs<R> a) {
     __syncwarp();
     auto src = packed(stg + SLOT * Sh::SS);
     auto dst = [&](int bb, int r, int, C v) { dstarr[bb + r * NBL] = v; };
-    fft_column<Plan, +1, Sh::PSH>(t, src, dst, xcol, tw, ws);
+    fft_column<Plan, +1, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
   };
   using I0 = std::integral_constant<int, 0>;
   using I1 = std::integral_constant<int, 1>;
@@ -357,7 +361,7 @@ __global__ void __launch_bounds__(128) kz_reg_mhd_kernel(const PassArgs<R> a) {
     constexpr int w = decltype(w_tag)::value;
     auto src = packed_g(yin + (9 + w) * g.sY);
     auto dst = [&](int bb, int r, int, C v) { z[bb + r * NBL] = v; };
-    fft_column<Plan, +1, Sh::PSH>(t, src, dst, xcol, tw, ws);
+    fft_column<Plan, +1, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
     constexpr int c1 = (w + 1) % 3, c2 = (w + 2) % 3;
 #pragma unroll
     for (int q = 0; q < E; ++q) {
@@ -439,7 +443,7 @@ __global__ void __launch_bounds__(128) kz_reg_adj_kernel(const PassArgs<R> a) {
   C z[E];
   auto forward_store = [&](auto& src, int c) {
     auto dst = [&](int b, int r, int, C v) { z[b + r * NBL] = v; };
-    fft_column<Plan, -1, Sh::PSH>(t, src, dst, xcol, tw, ws);
+    fft_column<Plan, -1, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
     C zm[E];
     const int src_lane = (P - t) % P;
 #pragma unroll
@@ -466,7 +470,7 @@ __global__ void __launch_bounds__(128) kz_reg_adj_kernel(const PassArgs<R> a) {
     __syncwarp();
     auto src = packed(stg + SLOT * Sh::SS);
     auto dst = [&](int bb, int r, int, C v) { dstarr[bb + r * NBL] = v; };
-    fft_column<Plan, +1, Sh::PSH>(t, src, dst, xcol, tw, ws);
+    fft_column<Plan, +1, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
   };
   inv_to(std::integral_constant<int, 0>(), std::integral_constant<int, 8>(), av[0]);
   inv_to(std::integral_constant<int, 1>(), std::integral_constant<int, 7>(), av[1]);
@@ -601,10 +605,10 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT) kx_reg_kernel(const Pass
     constexpr int DIR = decltype(dir_tag)::value;
     if constexpr (GT > 32) {
       const NamedSync ns{1 + grp, GT};
-      fft_column<Plan, DIR, Sh::PSH>(t, src, dst, xcol, tw, ns);
+      fft_column<Plan, DIR, Sh::PSH, false>(t, src, dst, xcol, tw, ns);
     } else {
       const WarpSync ws;
-      fft_column<Plan, DIR, Sh::PSH>(t, src, dst, xcol, tw, ws);
+      fft_column<Plan, DIR, Sh::PSH, false>(t, src, dst, xcol, tw, ws);
     }
   };
   using Fwd = std::integral_constant<int, -1>;
@@ -722,10 +726,10 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT) kx_reg_adj_kernel(const 
     constexpr int DIR = decltype(dir_tag)::value;
     if constexpr (GT > 32) {
       const NamedSync ns{1 + grp, GT};
-      fft_column<Plan, DIR, Sh::PSH>(t, src, dst, xcol, tw, ns);
+      fft_column<Plan, DIR, Sh::PSH, false>(t, src, dst, xcol, tw, ns);
     } else {
       const WarpSync ws;
-      fft_column<Plan, DIR, Sh::PSH>(t, src, dst, xcol, tw, ws);
+      fft_column<Plan, DIR, Sh::PSH, false>(t, src, dst, xcol, tw, ws);
     }
   };
   using Fwd = std::integral_constant<int, -1>;
