@@ -192,11 +192,17 @@ int64_t tg_last_launch_count(const tg_plan* plan);
  * loss = enstrophy of the final state (jax/taylor_green_jax.py:112-115 applied at
  * t_final).  Writes loss (device double), grad_state = dloss/dstate0 (device, state
  * layout; the gradient for the inner product sum_half w Re(a conj b), w = 1 at
- * kz = 0 and 2 otherwise) and grad_nu = dloss/dnu (device double).  States are
- * checkpointed every checkpoint_every steps (<= 0: ceil(sqrt(nsteps))) and each
- * segment is recomputed once on the way back.  The reference has no adjoint; its
- * autodiff counterpart is jax.grad through jax/taylor_green_jax.py:188-196.
- * Allocates its work buffers for the call and synchronises the stream. */
+ * kz = 0 and 2 otherwise) and grad_nu = dloss/dnu (device double).
+ * checkpoint_every > 0: states are checkpointed every checkpoint_every steps and each
+ * segment is recomputed on the way back; 0: every ceil(sqrt(nsteps)) steps.
+ * TG_ADJ_HOST_TAPE: one forward sweep records every step's state and stage nonlinear
+ * terms in pinned host memory (4 states per step, kept by the plan for later calls) and
+ * nothing is recomputed; FP32 plans with register passes (n = 16 ... 256), else (or if
+ * the host memory cannot be pinned) the sqrt(nsteps) checkpointing runs instead.
+ * The reference has no adjoint; its autodiff counterpart is jax.grad through
+ * jax/taylor_green_jax.py:188-196.  Allocates its device work buffers for the call and
+ * synchronises the stream. */
+#define TG_ADJ_HOST_TAPE (-1)
 int tg_adjoint(tg_plan* plan, const void* state0, double dt, double nu, int nsteps, int checkpoint_every,
                void* grad_state, double* grad_nu, double* loss);
 

@@ -24,6 +24,7 @@ TG_DERIVED_VORTICITY, TG_DERIVED_DIVERGENCE = 0, 1
 TG_DIAG_WIDTH = 8
 TG_PROF_SLOTS = 12
 TG_NOALLOC_MAX_RUNS = 64
+TG_ADJ_HOST_TAPE = -1  # tg_adjoint: keep every step's stage data in pinned host memory
 PASS_NAMES = ("kx_stage_hd", "kx_stage_mhd", "kx_load_hd", "kx_load_mhd", "kx_fwd_hd",
               "kx_fwd_mhd", "ky_inverse", "ky_forward", "kz_product_hd", "kz_product_mhd",
               "kz_c2r", "kz_r2c")

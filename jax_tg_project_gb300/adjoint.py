@@ -35,7 +35,8 @@ class _FinalEnstrophy(torch.autograd.Function):
         n = int(u0.shape[-1])
         plan = rt.get_plan(n, precision=precision)
         s0 = plan.forward(rt.as_physical(u0.detach(), plan, 3))
-        loss, grad, gnu = plan.adjoint(s0, float(dt), float(nu), int(nsteps), int(checkpoint_every))
+        ck = checkpoint_every if checkpoint_every == "tape" else int(checkpoint_every)
+        loss, grad, gnu = plan.adjoint(s0, float(dt), float(nu), int(nsteps), ck)
         # d loss / d u0 on the grid: the state gradient mapped back through the
         # dealiased forward transform, (1/n^3) F^-1 grad
         gu = plan.inverse(grad)[0] / float(n) ** 3

@@ -499,6 +499,22 @@ __global__ void __launch_bounds__(kDiagThreads) adj_dnu_partial(const cplx<R>* L
   if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
+// acc += fixed-order sum of n partials with one block of 256 threads: strided thread
+// sums, a shuffle tree per warp, then the eight warp sums in turn
+__global__ void __launch_bounds__(256) accumulate_partials_wide(const double* part, int n, double* acc) {
+  __shared__ double ws[8];
+  double v = 0.0;
+  for (int b = threadIdx.x; b < n; b += 256) v += part[b];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += ws[w];
+    *acc += t;
+  }
+}
+
 // acc += fixed-order sum of nblk partials (one warp: strided lane sums, then a fixed
 // shuffle tree, so the result does not depend on scheduling)
 __global__ void accumulate_partials(const double* part, int nblk, double* acc) {
@@ -625,7 +641,10 @@ struct tg_plan {
   cudaStream_t cap = nullptr;  // private non-blocking stream used only to capture the step graph
   void* X = nullptr;    // [batch][G][N][M][Hz]
   void* Y = nullptr;    // [batch][G][N][N][Hz]; W aliases it
-  void* Z = nullptr;    // [batch][F][N][N][Hz]
+  void* Z = nullptr;    // [batch][F][N][N][Hz], right after Y in the same allocation
+  void* tape = nullptr; // adjoint step tape written by the x stage kernels (batch 1), or null
+  void* htape = nullptr;   // pinned host memory of the adjoint tape, kept for later calls
+  size_t htape_bytes = 0;
   void* ACC = nullptr;  // [batch][F][M][M][Hz]
   void* VS = nullptr;   // explicit-viscosity stage state
   void* TW = nullptr;   // W_N^m
@@ -724,6 +743,7 @@ struct Ops {
     a.S = static_cast<C*>(S);
     a.acc = static_cast<C*>(p->ACC);
     a.vs = static_cast<C*>(p->VS);
+    a.tape = static_cast<C*>(p->tape);
     a.stage = stage;
     a.nin = p->F;
     a.nout = p->G;
@@ -995,8 +1015,9 @@ int tg_plan_create(tg_plan** out, const tg_desc* d) {
   const size_t B = (size_t)p->batch;
   struct Alloc { void** ptr; size_t bytes; } allocs[] = {
       {&p->X, cs * B * p->G * g.sX},
-      {&p->Y, cs * B * p->G * g.sY},
-      {&p->Z, cs * B * p->F * g.sY},
+      // Y and Z in one block, Z right after Y: with batch 1 the block is also the
+      // contiguous nine-field buffer of the adjoint's in-place z pass
+      {&p->Y, cs * B * (p->G + p->F) * g.sY},
       {&p->ACC, cs * B * p->F * g.sS},
       {&p->VS, (p->flags & TG_FLAG_EXPLICIT_VISC) ? cs * B * p->F * g.sS : 0},
       {&p->TW, cs * n},
@@ -1014,6 +1035,7 @@ int tg_plan_create(tg_plan** out, const tg_desc* d) {
     }
     p->scratch += (int64_t)a.bytes;
   }
+  p->Z = static_cast<char*>(p->Y) + cs * B * p->G * g.sY;
   // twiddles W_N^m = exp(-2 pi i m / N), generated in FP64
   std::vector<double> tw(2 * (size_t)n);
   for (int m = 0; m < n; ++m) {
@@ -1054,7 +1076,8 @@ int tg_plan_destroy(tg_plan* p) {
   if (!p) return TG_OK;
   drop_graph(p);
   if (p->cap) cudaStreamDestroy(p->cap);
-  void* bufs[] = {p->X, p->Y, p->Z, p->ACC, p->VS, p->TW, p->part, p->dtmp, p->amax, p->coef};
+  if (p->htape) cudaFreeHost(p->htape);
+  void* bufs[] = {p->X, p->Y, p->ACC, p->VS, p->TW, p->part, p->dtmp, p->amax, p->coef};  // Z lies in Y's block
   for (void* b : bufs)
     if (b) cudaFree(b);
   delete p;
@@ -1319,6 +1342,7 @@ struct Adjoint {
   static constexpr int kDnuBlocks = 1024;
 
   ~Adjoint() {
+    release_tape();
     for (void* b : bufs) cudaFree(b);
   }
   int alloc(void** ptr, size_t bytes) {
@@ -1473,6 +1497,234 @@ struct Adjoint {
     return launch_check("adjoint combine");
   }
 
+  // ---------------------------------------------------------------- stage tape
+  // One graph-launched forward sweep in which the x stage kernels also write, per step,
+  // the input state V and the stage nonlinear terms n1, n2, n3 into one of two device
+  // slots; a copy stream moves every slot to pinned host memory.  The backward sweep
+  // streams the tape back (each buffer refilled as soon as its last reader has run)
+  // and runs the four adjoint stages of each step with no state recomputed:
+  //   stage s:  x (mu_s = seeds of L, g_{s+1}; a = P mu_s) -> y -> x (u, omega of the
+  //             stage state a_s, formed from V and n_{s-1}) -> y -> z (in place, nine
+  //             fields in the plan's Y|Z block) -> y -> x (g_s; lam accumulated)
+  //             -> d/dnu partial sums
+  // Device memory beyond the plan: the two slots (eight states, reused by the backward
+  // sweep as V[2], n1, n2, n3, L, lam, g), the working state and the partial sums.
+  std::vector<cudaEvent_t> evs;
+  cudaStream_t cs = nullptr;
+  cudaGraphExec_t gx[2] = {nullptr, nullptr};
+  cudaGraph_t gg[2] = {nullptr, nullptr};
+  cudaEvent_t event() {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess) evs.push_back(e);
+    return e;
+  }
+  void release_tape() {
+    for (int k = 0; k < 2; ++k) {
+      if (gx[k]) cudaGraphExecDestroy(gx[k]);
+      if (gg[k]) cudaGraphDestroy(gg[k]);
+      gx[k] = nullptr;
+      gg[k] = nullptr;
+    }
+    if (cs) cudaStreamSynchronize(cs);
+    for (cudaEvent_t e : evs) cudaEventDestroy(e);
+    evs.clear();
+    if (cs) cudaStreamDestroy(cs);
+    cs = nullptr;
+  }
+  // capture stages(S) with the tape pointer set (the step graph of one tape slot)
+  int capture(int k, C* S, C* tape) {
+    if (!p->cap) TG_CUDA(cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking), "capture stream");
+    cudaStream_t user = p->st;
+    TG_CUDA(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal), "begin capture");
+    const int64_t before = p->launches;
+    p->st = p->cap;
+    p->tape = tape;
+    int rc = Ops<R>::stages(p, S);
+    p->tape = nullptr;
+    p->st = user;
+    p->launches = before;
+    cudaError_t e = cudaStreamEndCapture(p->cap, &gg[k]);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "tape end capture");
+    TG_CUDA(cudaGraphInstantiate(&gx[k], gg[k], 0), "tape graph instantiate");
+    return TG_OK;
+  }
+  // one adjoint stage s of the step whose tape is tp = (V, n1, n2, n3); the stage's
+  // d(loss)/d(nu) partial sums go to part (one per CTA of the adjoint forward x pass)
+  int tape_stage(int s, const C* const tp[4], const C* L, C* LA, C* Gb, double* part, cudaEvent_t state_read) {
+    int rc;
+    const Geo& g = p->g;
+    C* X = static_cast<C*>(p->X);
+    C* Y = static_cast<C*>(p->Y);
+    PassArgs<R> a = Ops<R>::base(p);
+    a.flags |= FLAG_TAPE;
+    a.stage = s;
+    for (int i = 0; i < 4; ++i) a.tp[i] = tp[i];
+    a.S = const_cast<C*>(L);
+    a.acc = Gb;
+    // u, omega of a_s -> X[0..5]; a = P mu_s -> the first three field slots of Y (read by the
+    // three-field y pass below before the six-field y pass overwrites them)
+    a.out = X;
+    a.out2 = Y;
+    a.nin = 6;
+    a.nout = 9;
+    if ((rc = Ops<R>::go(p, OP_KX_ADJ_LOAD, a, "kx adjoint load"))) return rc;
+    if (state_read) TG_CUDA(cudaEventRecord(state_read, p->st), "event record");
+    PassArgs<R> b = Ops<R>::base(p);
+    b.in = Y;  // x-pass layout (field stride sX)
+    b.out = Y + 6 * g.sY;
+    b.nin = b.nout = 3;
+    if ((rc = Ops<R>::go(p, OP_KY_INV, b, "ky adjoint inverse (a)"))) return rc;
+    b = Ops<R>::base(p);
+    b.in = X;
+    b.out = Y;
+    b.nin = b.nout = 6;
+    if ((rc = Ops<R>::go(p, OP_KY_INV, b, "ky adjoint inverse (u, omega)"))) return rc;
+    b = Ops<R>::base(p);
+    b.in = Y;
+    b.out = Y;  // in place: p, q over u, omega
+    b.nin = 9;
+    b.nout = 6;
+    if ((rc = Ops<R>::go(p, OP_KZ_ADJ, b, "kz adjoint"))) return rc;
+    b = Ops<R>::base(p);
+    b.in = Y;
+    b.out = X;
+    b.nin = b.nout = 6;
+    if ((rc = Ops<R>::go(p, OP_KY_FWD, b, "ky adjoint forward"))) return rc;
+    b = Ops<R>::base(p);
+    b.flags |= FLAG_TAPE;
+    b.stage = s;
+    for (int i = 0; i < 4; ++i) b.tp[i] = tp[i];
+    b.in = X;
+    b.S = const_cast<C*>(L);
+    b.vs = LA;
+    b.spec_out = Gb;
+    b.part = part;
+    b.nin = 6;
+    return Ops<R>::go(p, OP_KX_ADJ_FWD, b, "kx adjoint forward");
+  }
+  int run_tape(const void* state0, double dt, double nu, int nsteps, void* grad, double* grad_nu, double* loss) {
+    int rc;
+    const Geo& g = p->g;
+    cudaStream_t st = p->st;
+    fbytes = sizeof(C) * 3 * (size_t)g.sS;
+    const size_t sN = 3 * (size_t)g.sS;  // elements of one state
+    const size_t need = (size_t)nsteps * 4 * fbytes;
+    if (p->htape_bytes < need) {
+      if (p->htape) cudaFreeHost(p->htape);
+      p->htape = nullptr;
+      p->htape_bytes = 0;
+      cudaError_t e = cudaHostAlloc(&p->htape, need, cudaHostAllocDefault);
+      if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        p->htape = nullptr;
+        return TG_E_NOMEM;  // the caller falls back to checkpointing
+      }
+      p->htape_bytes = need;
+    }
+    C* host = static_cast<C*>(p->htape);
+    C *slot = nullptr, *cur0 = nullptr;
+    if ((rc = alloc((void**)&slot, 8 * fbytes))) return rc;
+    if ((rc = alloc((void**)&cur0, fbytes))) return rc;
+    if ((rc = alloc((void**)&dnu, sizeof(double)))) return rc;
+    // partial sums: stages 4, 3, 2, one slot per CTA of the x pass (at most M x Hk CTAs);
+    // slots a smaller grid leaves unwritten stay zero
+    const size_t pslots = (size_t)g.M * g.Hk;
+    if ((rc = alloc((void**)&dpart, sizeof(double) * 3 * pslots))) return rc;
+    TG_CUDA(cudaMemsetAsync(dpart, 0, sizeof(double) * 3 * pslots, st), "memset");
+    blocks = (int)std::min<long long>(((long long)g.M * g.M * g.Hk + 255) / 256, 2048);
+    TG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "copy stream");
+    cudaEvent_t written[2] = {event(), event()}, copied[2] = {event(), event()};
+    for (cudaEvent_t e : evs)
+      if (!e) return fail(TG_E_CUDA, "tg_adjoint: event creation failed");
+    C* tslot[2] = {slot, slot + 4 * sN};
+    auto offload = [&](int j, int k) -> int {
+      TG_CUDA(cudaEventRecord(written[k], st), "event record");
+      TG_CUDA(cudaStreamWaitEvent(cs, written[k], 0), "stream wait");
+      TG_CUDA(cudaMemcpyAsync(host + (size_t)j * 4 * sN, tslot[k], 4 * fbytes, cudaMemcpyDeviceToHost, cs),
+              "tape offload");
+      TG_CUDA(cudaEventRecord(copied[k], cs), "event record");
+      return TG_OK;
+    };
+    // forward sweep: step 0 eagerly (sets kernel attributes outside capture), then graphs
+    TG_CUDA(cudaMemcpyAsync(cur0, state0, fbytes, cudaMemcpyDeviceToDevice, st), "state copy");
+    if ((rc = Ops<R>::start(p, cur0))) return rc;
+    p->tape = tslot[0];
+    rc = Ops<R>::stages(p, cur0);
+    p->tape = nullptr;
+    if (rc) return rc;
+    if ((rc = offload(0, 0))) return rc;
+    if (nsteps > 1) {
+      if ((rc = capture(0, cur0, tslot[0]))) return rc;
+      if ((rc = capture(1, cur0, tslot[1]))) return rc;
+    }
+    for (int j = 1; j < nsteps; ++j) {
+      const int k = j & 1;
+      if (j >= 2) TG_CUDA(cudaStreamWaitEvent(st, copied[k], 0), "stream wait");
+      TG_CUDA(cudaGraphLaunch(gx[k], st), "tape graph launch");
+      p->launches += 16;
+      if ((rc = offload(j, k))) return rc;
+    }
+    // loss and its gradient; the slots become the backward buffers once offloaded
+    if ((rc = Ops<R>::diagnostics(p, cur0, p->dtmp))) return rc;
+    copy_double<<<1, 32, 0, st>>>(p->dtmp + TG_D_ENSTROPHY, loss);
+    TG_CUDA(cudaStreamWaitEvent(st, copied[0], 0), "stream wait");
+    TG_CUDA(cudaStreamWaitEvent(st, copied[1], 0), "stream wait");
+    C* Vb[2] = {slot, slot + sN};
+    C* N1 = slot + 2 * sN;
+    C* N2 = slot + 3 * sN;
+    C* N3 = slot + 4 * sN;
+    C* L = slot + 5 * sN;
+    C* LA = slot + 6 * sN;
+    C* Gb = slot + 7 * sN;
+    enstrophy_grad_kernel<R><<<blocks, 256, 0, st>>>(cur0, L, g);
+    TG_CUDA(cudaMemsetAsync(dnu, 0, sizeof(double), st), "memset");
+    if ((rc = launch_check("loss gradient"))) return rc;
+    // refill events: the tape buffers are reloaded once their last reader has run
+    cudaEvent_t n3_free = event(), n2_free = event(), n1_free = event(), v_free[2] = {event(), event()};
+    cudaEvent_t n3_ready = event(), n2_ready = event(), n1_ready = event(), v_ready[2] = {event(), event()};
+    for (cudaEvent_t e : evs)
+      if (!e) return fail(TG_E_CUDA, "tg_adjoint: event creation failed");
+    TG_CUDA(cudaEventRecord(v_free[0], st), "event record");  // the slots are free from here on
+    TG_CUDA(cudaEventRecord(v_free[1], st), "event record");
+    TG_CUDA(cudaEventRecord(n1_free, st), "event record");
+    TG_CUDA(cudaEventRecord(n2_free, st), "event record");
+    TG_CUDA(cudaEventRecord(n3_free, st), "event record");
+    auto fetch = [&](int j) -> int {
+      const C* src = host + (size_t)j * 4 * sN;
+      struct { C* dst; size_t off; cudaEvent_t free_, ready; } items[] = {
+          {N3, 3, n3_free, n3_ready}, {N2, 2, n2_free, n2_ready}, {N1, 1, n1_free, n1_ready},
+          {Vb[j & 1], 0, v_free[j & 1], v_ready[j & 1]}};
+      for (auto& it : items) {
+        TG_CUDA(cudaStreamWaitEvent(cs, it.free_, 0), "stream wait");
+        TG_CUDA(cudaMemcpyAsync(it.dst, src + it.off * sN, fbytes, cudaMemcpyHostToDevice, cs), "tape fetch");
+        TG_CUDA(cudaEventRecord(it.ready, cs), "event record");
+      }
+      return TG_OK;
+    };
+    if ((rc = fetch(nsteps - 1))) return rc;
+    for (int j = nsteps - 1; j >= 0; --j) {
+      const C* tp[4] = {Vb[j & 1], N1, N2, N3};
+      for (cudaEvent_t e : {v_ready[j & 1], n1_ready, n2_ready, n3_ready})
+        TG_CUDA(cudaStreamWaitEvent(st, e, 0), "stream wait");
+      if ((rc = tape_stage(4, tp, L, LA, Gb, dpart, nullptr))) return rc;
+      TG_CUDA(cudaEventRecord(n3_free, st), "event record");
+      if ((rc = tape_stage(3, tp, L, LA, Gb, dpart + pslots, n2_free))) return rc;
+      if ((rc = tape_stage(2, tp, L, LA, Gb, dpart + 2 * pslots, nullptr))) return rc;
+      TG_CUDA(cudaEventRecord(n1_free, st), "event record");
+      if ((rc = tape_stage(1, tp, L, LA, Gb, nullptr, v_free[j & 1]))) return rc;
+      accumulate_partials_wide<<<1, 256, 0, st>>>(dpart, (int)(3 * pslots), dnu);
+      ++p->launches;
+      if ((rc = launch_check("adjoint nu sum"))) return rc;
+      std::swap(L, LA);
+      if (j > 0 && (rc = fetch(j - 1))) return rc;
+    }
+    TG_CUDA(cudaMemcpyAsync(grad, L, fbytes, cudaMemcpyDeviceToDevice, st), "grad copy");
+    TG_CUDA(cudaMemcpyAsync(grad_nu, dnu, sizeof(double), cudaMemcpyDeviceToDevice, st), "grad_nu copy");
+    TG_CUDA(cudaStreamSynchronize(st), "adjoint sync");
+    return TG_OK;
+  }
+
   int run(const void* state0, double dt, double nu, int nsteps, int seglen, void* grad, double* grad_nu,
           double* loss) {
     int rc;
@@ -1526,6 +1778,18 @@ extern "C" int tg_adjoint(tg_plan* p, const void* state0, double dt, double nu, 
     return fail(TG_E_INVALID, "tg_adjoint: need dt > 0, nu >= 0 and nsteps >= 1");
   if (p->flags & TG_FLAG_EXPLICIT_VISC)
     return fail(TG_E_UNSUPPORTED, "tg_adjoint: differentiates the integrating-factor RK4 only");
+  if (checkpoint_every == TG_ADJ_HOST_TAPE) {
+    if (p->prec == TG_PREC_F32 && has_reg_adjoint(p->n) && p->variant == 0) {
+      int rc = set_coefs(p, dt, nu, 0.0);
+      if (rc) return rc;
+      p->launches = 0;
+      Adjoint<float> A{p};
+      rc = A.run_tape(state0, dt, nu, nsteps, grad_state, grad_nu, loss);
+      if (rc != TG_E_NOMEM) return rc;
+      (void)cudaGetLastError();
+    }
+    checkpoint_every = 0;  // no tape kernels for this plan, or no memory for the tape
+  }
   int seglen = checkpoint_every > 0 ? checkpoint_every : (int)std::ceil(std::sqrt((double)nsteps));
   seglen = std::max(1, std::min(seglen, nsteps));
   int rc = set_coefs(p, dt, nu, 0.0);

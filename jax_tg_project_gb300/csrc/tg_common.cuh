@@ -75,10 +75,12 @@ template <typename R, int N, int BUFS = 7> struct LinesZ {
   static constexpr int value = fit(pref);
 };
 
-enum KxMode { KX_STAGE = 0, KX_LOAD = 1, KX_FWD = 2, KX_ADJ_LOAD = 3, KX_ADJ_FWD = 4, KX_NL_FWD = 5 };
+enum KxMode { KX_STAGE = 0, KX_LOAD = 1, KX_FWD = 2, KX_ADJ_LOAD = 3, KX_ADJ_FWD = 4, KX_NL_FWD = 5,
+              KX_ADJ_LOAD_T = 6, KX_ADJ_FWD_T = 7 };  // _T: the stage-tape forms (FLAG_TAPE)
 enum FieldMap { MAP_ID = 0, MAP_UW = 1, MAP_UWBJ = 2, MAP_DIV = 3, MAP_DIVB = 4, MAP_CURL = 5, MAP_ADJ = 6 };
 enum KzMode { KZ_PROD_HD = 0, KZ_PROD_MHD = 1, KZ_C2R = 2, KZ_R2C = 3, KZ_ADJ = 4 };
-enum Flags { FLAG_EXPLICIT = 1, FLAG_RHS = 2, FLAG_AMAX = 4, FLAG_NONLIN = 8, FLAG_ADJ = 16 };
+enum Flags { FLAG_EXPLICIT = 1, FLAG_RHS = 2, FLAG_AMAX = 4, FLAG_NONLIN = 8, FLAG_ADJ = 16,
+             FLAG_TAPE = 32 };  // FLAG_TAPE: adjoint stage kernels read the step tape
 
 template <typename R> struct PassArgs {
   Geo g;
@@ -99,6 +101,10 @@ template <typename R> struct PassArgs {
   int map;               // FieldMap for KX_LOAD
   int nin, nout;         // fields read / written by this pass
   int variant;           // 0: register-resident x/z passes where built, 1: shared-memory passes
+  cplx<R>* tape;         // KX_STAGE (batch 1): the step tape [V, n1, n2, n3], or null
+  const cplx<R>* tp[4];  // FLAG_TAPE adjoint stage kernels: the step tape V, n1, n2, n3
+  cplx<R>* out2;         // KX_ADJ_LOAD_T with nout = 9: the three a = P mu fields (x-pass layout)
+  double* part;          // KX_ADJ_FWD_T: per-CTA partial sums of d(loss)/d(nu) of the stage
 };
 
 // signed wavenumber of compact index i (0..M-1)

@@ -21,8 +21,13 @@ cudaError_t TG_CAT(launch, TG_REAL, TG_N)(int op, const PassArgs<TG_REAL>& a, in
     if (a.variant == 0 && op == OP_KZ_PROD_HD) return launch_kz_reg<TG_REAL, TG_N>(a, runs, st);
     if (a.variant == 0 && op == OP_KZ_PROD_MHD) return launch_kz_reg_mhd<TG_REAL, TG_N>(a, runs, st);
     if (a.variant == 0 && op == OP_KZ_ADJ) return launch_kz_reg_adj<TG_REAL, TG_N>(a, runs, st);
-    if (op == OP_KX_ADJ_LOAD) return launch_kx_reg_adj<TG_REAL, TG_N, KX_ADJ_LOAD>(a, runs, st);
-    if (op == OP_KX_ADJ_FWD) return launch_kx_reg_adj<TG_REAL, TG_N, KX_ADJ_FWD>(a, runs, st);
+    const bool tape = (a.flags & FLAG_TAPE) != 0;
+    if (op == OP_KX_ADJ_LOAD)
+      return tape ? launch_kx_reg_adj<TG_REAL, TG_N, KX_ADJ_LOAD_T>(a, runs, st)
+                  : launch_kx_reg_adj<TG_REAL, TG_N, KX_ADJ_LOAD>(a, runs, st);
+    if (op == OP_KX_ADJ_FWD)
+      return tape ? launch_kx_reg_adj<TG_REAL, TG_N, KX_ADJ_FWD_T>(a, runs, st)
+                  : launch_kx_reg_adj<TG_REAL, TG_N, KX_ADJ_FWD>(a, runs, st);
     if (op == OP_KX_NL_FWD) return launch_kx_reg_adj<TG_REAL, TG_N, KX_NL_FWD>(a, runs, st);
   }
   if constexpr (std::is_same<TG_REAL, float>::value && HasRegX<TG_N>::value) {

@@ -394,9 +394,11 @@ static cudaError_t launch_kz_reg_mhd(const PassArgs<R>& a, int runs, cudaStream_
 // ------------------------------------------------------------------ z pass, adjoint
 // Adjoint of u x omega for one line pair: inverse transforms of u, omega (state) and
 // a (projected adjoint field); outputs p = omega x a (fields 0..2) and q = a x u (3..5).
-// Order: a, u -> registers; q transformed straight from them; omega accumulates p.
+// Order: a -> registers; each u component accumulates q, which is then transformed
+// from the registers; each omega component accumulates p in the same registers.
+// At most a, one accumulator and one transform are live: three CTAs per SM.
 template <typename R, int N>
-__global__ void __launch_bounds__(128) kz_reg_adj_kernel(const PassArgs<R> a) {
+__global__ void __launch_bounds__(128, 3) kz_reg_adj_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Sh = KzRegMhdShape<R, N>;  // same footprint: 9 staged fields per pair
   using Plan = typename Sh::Plan;
@@ -417,7 +419,7 @@ __global__ void __launch_bounds__(128) kz_reg_adj_kernel(const PassArgs<R> a) {
   // slots in order of use: a (fields 6,7,8), u (0,1,2), omega (3,4,5)
 #pragma unroll
   for (int i = 0; i < 9; ++i) {
-    const int f = (i < 3) ? i + 6 : ((i < 6) ? i - 3 : i - 3);
+    const int f = (i < 3) ? i + 6 : i - 3;
     const C* src = yin + f * g.sY + row0;
     C* dst = stg + i * Sh::SS;
     for (int c = t; c < Hz; c += P) cp_async16(dst + 2 * c, src + 2 * c);
@@ -463,7 +465,7 @@ __global__ void __launch_bounds__(128) kz_reg_adj_kernel(const PassArgs<R> a) {
       }
     }
   };
-  C av[3][E], u[3][E];
+  C av[3][E], pm[3][E];
   auto inv_to = [&](auto slot_tag, auto wait_tag, auto* dstarr) {
     constexpr int SLOT = decltype(slot_tag)::value;
     cp_async_wait<decltype(wait_tag)::value>();
@@ -475,22 +477,37 @@ __global__ void __launch_bounds__(128) kz_reg_adj_kernel(const PassArgs<R> a) {
   inv_to(std::integral_constant<int, 0>(), std::integral_constant<int, 8>(), av[0]);
   inv_to(std::integral_constant<int, 1>(), std::integral_constant<int, 7>(), av[1]);
   inv_to(std::integral_constant<int, 2>(), std::integral_constant<int, 6>(), av[2]);
-  inv_to(std::integral_constant<int, 3>(), std::integral_constant<int, 5>(), u[0]);
-  inv_to(std::integral_constant<int, 4>(), std::integral_constant<int, 4>(), u[1]);
-  inv_to(std::integral_constant<int, 5>(), std::integral_constant<int, 3>(), u[2]);
-  {  // q = a x u -> fields 3..5
-    auto q0 = [&](int, int q) -> C { return mk<C>(av[1][q].x * u[2][q].x - av[2][q].x * u[1][q].x,
-                                                  av[1][q].y * u[2][q].y - av[2][q].y * u[1][q].y); };
-    auto q1 = [&](int, int q) -> C { return mk<C>(av[2][q].x * u[0][q].x - av[0][q].x * u[2][q].x,
-                                                  av[2][q].y * u[0][q].y - av[0][q].y * u[2][q].y); };
-    auto q2 = [&](int, int q) -> C { return mk<C>(av[0][q].x * u[1][q].x - av[1][q].x * u[0][q].x,
-                                                  av[0][q].y * u[1][q].y - av[1][q].y * u[0][q].y); };
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int q = 0; q < E; ++q) pm[c][q] = czero<C>();
+  // q = a x u:  q_{w+1} += a_{w+2} u_w;  q_{w+2} -= a_{w+1} u_w
+  auto add_u = [&](auto w_tag, auto wait_tag) {
+    constexpr int w = decltype(w_tag)::value;
+    inv_to(std::integral_constant<int, 3 + w>(), wait_tag, z);
+    constexpr int c1 = (w + 1) % 3, c2 = (w + 2) % 3;
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      pm[c1][q] = mk<C>(pm[c1][q].x + av[c2][q].x * z[q].x, pm[c1][q].y + av[c2][q].y * z[q].y);
+      pm[c2][q] = mk<C>(pm[c2][q].x - av[c1][q].x * z[q].x, pm[c2][q].y - av[c1][q].y * z[q].y);
+    }
+  };
+  add_u(std::integral_constant<int, 0>(), std::integral_constant<int, 5>());
+  add_u(std::integral_constant<int, 1>(), std::integral_constant<int, 4>());
+  add_u(std::integral_constant<int, 2>(), std::integral_constant<int, 3>());
+  // every input row of this pair is in shared memory before the first output store, so
+  // the outputs may overwrite the inputs (out == in: the pass runs in place)
+  cp_async_wait_all();
+  __syncwarp();
+  {
+    auto q0 = [&](int, int q) -> C { return pm[0][q]; };
+    auto q1 = [&](int, int q) -> C { return pm[1][q]; };
+    auto q2 = [&](int, int q) -> C { return pm[2][q]; };
     forward_store(q0, 3);
     forward_store(q1, 4);
     forward_store(q2, 5);
   }
   // p = omega x a:  (omega x a)_{w+1} -= omega_w a_{w+2};  (omega x a)_{w+2} += omega_w a_{w+1}
-  C pm[3][E];
 #pragma unroll
   for (int c = 0; c < 3; ++c)
 #pragma unroll
@@ -549,8 +566,8 @@ struct KxRegShape {
 
 
 // one of the six inverse-transformed fields u, curl u from the column's state
-template <int GI, typename C, int E>
-__device__ __forceinline__ C uw_field(const C (&v)[3][E], int q, float kx, float ky, float kz) {
+template <int GI, typename A>
+__device__ __forceinline__ auto uw_field(const A& v, int q, float kx, float ky, float kz) {
   if constexpr (GI < 3) {
     return v[GI][q];
   } else {
@@ -626,10 +643,18 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT) kx_reg_kernel(const Pass
   } else {
     const R inv_n3 = R(1) / (R(N) * R(N) * R(N));
     const C* win = a.in + (long long)run * 3 * g.sX + (long long)iyc * Hz + kz;
+    // issue the global loads of all three fields before the first transform (the
+    // first pass of thread t reads x = t + P q into slot q), so that their latency
+    // is paid once; the slots are consumed field by field
+    C pre[3][E];
+#pragma unroll
+    for (int f = 0; f < 3; ++f)
+#pragma unroll
+      for (int q = 0; q < E; ++q)
+        pre[f][q] = zok ? win[f * g.sX + (long long)(t + P * q) * M * Hz] : czero<C>();
 #pragma unroll
     for (int f = 0; f < 3; ++f) {
-      const C* wf = win + f * g.sX;
-      auto src = [&](int x, int) -> C { return zok ? wf[(long long)x * M * Hz] : czero<C>(); };
+      auto src = [&](int, int q) -> C { return pre[f][q]; };
       auto dst = [&](int b, int r, int, C val) { v[f][b + r * NBL] = cscale(val, inv_n3); };
       run_fft(src, dst, Fwd());
     }
@@ -656,6 +681,10 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT) kx_reg_kernel(const Pass
         for (int f = 0; f < 3; ++f) {
           const long long o = soff + ((long long)f * M + ic) * M * Hz;
           const C s = stg[((long long)f * M + ic) * QW + col];
+          if (a.tape != nullptr) {  // adjoint tape (batch 1): n_stage for stages 1..3, V at stage 1
+            if (a.stage <= 3) a.tape[(long long)a.stage * 3 * g.sS + o] = v[f][q];
+            if (a.stage == 1) a.tape[o] = s;
+          }
           C acc = (a.stage > 1) ? stg[((long long)(3 + f) * M + ic) * QW + col] : czero<C>();
           const C vs = (expl && a.stage > 1) ? a.vs[o] : s;
           const C nv = rk4_combine<C>(a.stage, expl, v[f][q], s, acc, vs, h, lin);
@@ -702,7 +731,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT) kx_reg_kernel(const Pass
 //              -> 9 fields (u 0..2, omega 3..5, a 6..8)
 // KX_ADJ_FWD:  forward-x of p (0..2), q (3..5) -> spec_out = F p + i k x F q (1/N^3 applied)
 template <typename R, int N, int MODE>
-__global__ void __launch_bounds__(KxRegShape<R, N>::NT) kx_reg_adj_kernel(const PassArgs<R> a) {
+__global__ void __launch_bounds__(KxRegShape<R, N>::NT, 2) kx_reg_adj_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Sh = KxRegShape<R, N>;
   using Plan = typename Sh::Plan;
@@ -734,47 +763,124 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT) kx_reg_adj_kernel(const 
   };
   using Fwd = std::integral_constant<int, -1>;
   using Inv = std::integral_constant<int, +1>;
-  if constexpr (MODE == KX_ADJ_LOAD) {
-    C v[3][E], w[3][E];
-#pragma unroll
-    for (int q = 0; q < E; ++q) {
-      const int ic = kcompact(t + P * q, N, K);
-      const bool ok = zok && ic >= 0;
-#pragma unroll
-      for (int f = 0; f < 3; ++f) {
-        const long long o = soff + ((long long)f * M + (ok ? ic : 0)) * M * Hz;
-        v[f][q] = ok ? a.spec_in[o] : czero<C>();
-        w[f][q] = ok ? a.S[o] : czero<C>();
-      }
-      if (ok) {
-        const float kx = float(ksigned(ic, K));
-        leray(w[0][q], w[1][q], w[2][q], kx, kyf, kzf, kx * kx + kyf * kyf + kzf * kzf);
-      }
-    }
-    C* xo = a.out + (long long)run * 9 * g.sX + (long long)iyc * Hz + kz;
-    auto inverse = [&](auto gi_tag) {
+  constexpr bool TAPE = (MODE == KX_ADJ_LOAD_T || MODE == KX_ADJ_FWD_T);
+  if constexpr (MODE == KX_ADJ_LOAD || MODE == KX_ADJ_LOAD_T) {
+    // a = P mu first (its three transforms retire w), then u, curl u of the state:
+    // only one three-field array is live at a time.  nout = 9 writes both into fields
+    // 0..8 (u, omega, a); nout = 3 only a (into fields 0..2), nout = 6 only u, omega.
+    // KX_ADJ_LOAD_T: the stage state and mu are formed here from the step tape:
+    //   state a_s from V (tp[0]) and n_{s-1} (tp[s-1]) by the Lawson stage formula,
+    //   mu_s = cl L + cg g_{s+1} (L in S, g_{s+1} in acc) with the adjoint seeds of the tableau.
+    constexpr bool tape = TAPE;
+    const RunCoef cf = a.coef[run];
+    const R h = R(cf.dt);
+    const int st = a.stage;
+    C* xo = a.out + (long long)run * a.nout * g.sX + (long long)iyc * Hz + kz;
+    const int gi0 = (a.nout == 3) ? 6 : 0;  // output field of GI = gi0 + slot
+    // KX_ADJ_LOAD_T with nout = 9: u, omega into out (6 fields), a into out2 (3 fields)
+    C* xa = (TAPE && a.nout == 9) ? a.out2 + (long long)iyc * Hz + kz - 6 * g.sX : xo - gi0 * g.sX;
+    auto inverse_from = [&](auto gi_tag, auto* arr) {
       constexpr int GI = decltype(gi_tag)::value;
       auto src = [&](int k, int q) -> C {
         const int ic = kcompact(k, N, K);
         if (ic < 0) return czero<C>();
-        if constexpr (GI < 6) return uw_field<GI>(v, q, float(ksigned(ic, K)), kyf, kzf);
-        else return w[GI - 6][q];
+        if constexpr (GI < 6) return uw_field<GI>(arr, q, float(ksigned(ic, K)), kyf, kzf);
+        else return arr[GI - 6][q];
       };
-      C* xg = xo + GI * g.sX;
+      C* xg = (GI >= 6) ? xa + GI * g.sX : xo + (GI - gi0) * g.sX;
       auto dst = [&](int, int, int xx, C val) {
         if (zok) xg[(long long)xx * M * Hz] = val;
       };
       run_fft(src, dst, Inv());
     };
-    inverse(std::integral_constant<int, 0>());
-    inverse(std::integral_constant<int, 1>());
-    inverse(std::integral_constant<int, 2>());
-    inverse(std::integral_constant<int, 3>());
-    inverse(std::integral_constant<int, 4>());
-    inverse(std::integral_constant<int, 5>());
-    inverse(std::integral_constant<int, 6>());
-    inverse(std::integral_constant<int, 7>());
-    inverse(std::integral_constant<int, 8>());
+    // Lawson factors expm1(-nu k^2 h), expm1(-nu k^2 h / 2) of mode (ic, iyc, kz)
+    auto factors = [&](int ic, R& m1, R& mh) {
+      const float kx = float(ksigned(ic, K));
+      const R lin = R(cf.nu * double(kx * kx + kyf * kyf + kzf * kzf));
+      m1 = rexpm1<R>(-lin * h);
+      mh = rexpm1<R>(R(-0.5) * lin * h);
+    };
+    // mu (projected) into w: plain S, or the tape seeds cl L + cg g
+    auto load_mu = [&](auto* w) {
+#pragma unroll
+      for (int q = 0; q < E; ++q) {
+        const int ic = kcompact(t + P * q, N, K);
+        const bool ok = zok && ic >= 0;
+        R cl = R(1), cg = R(0);
+        if (tape && ok) {
+          R m1, mh;
+          factors(ic, m1, mh);
+          const R e1 = R(1) + m1, eh = R(1) + mh;
+          if (st == 4) { cl = h / R(6); }
+          else if (st == 3) { cl = h / R(3) * eh; cg = h * eh; }
+          else if (st == 2) { cl = h / R(3) * eh; cg = R(0.5) * h; }
+          else { cl = h / R(6) * e1; cg = R(0.5) * h * eh; }
+        }
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+          const long long o = soff + ((long long)f * M + (ok ? ic : 0)) * M * Hz;
+          C m = czero<C>();
+          if (ok) {
+            const C l = a.S[o];
+            m = mk<C>(cl * l.x, cl * l.y);
+            if (tape && st != 4) {
+              const C gp = a.acc[o];
+              m = mk<C>(m.x + cg * gp.x, m.y + cg * gp.y);
+            }
+          }
+          w[f][q] = m;
+        }
+        if (ok) {
+          const float kx = float(ksigned(ic, K));
+          leray(w[0][q], w[1][q], w[2][q], kx, kyf, kzf, kx * kx + kyf * kyf + kzf * kzf);
+        }
+      }
+    };
+    // the state whose u, curl u are transformed: spec_in, or the tape's stage state
+    auto load_state = [&](auto* v) {
+#pragma unroll
+      for (int q = 0; q < E; ++q) {
+        const int ic = kcompact(t + P * q, N, K);
+        const bool ok = zok && ic >= 0;
+        R m1 = R(0), mh = R(0);
+        if (tape && ok && st > 1) factors(ic, m1, mh);
+        const R eh = R(1) + mh;
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+          const long long o = soff + ((long long)f * M + (ok ? ic : 0)) * M * Hz;
+          C x = czero<C>();
+          if (ok) {
+            x = tape ? a.tp[0][o] : a.spec_in[o];
+            if (tape && st > 1) {
+              const C nn = a.tp[st - 1][o];
+              R dx, dy;
+              if (st == 2) { dx = mh * x.x + eh * R(0.5) * h * nn.x; dy = mh * x.y + eh * R(0.5) * h * nn.y; }
+              else if (st == 3) { dx = mh * x.x + R(0.5) * h * nn.x; dy = mh * x.y + R(0.5) * h * nn.y; }
+              else { dx = m1 * x.x + h * eh * nn.x; dy = m1 * x.y + h * eh * nn.y; }
+              x = mk<C>(x.x + dx, x.y + dy);
+            }
+          }
+          v[f][q] = x;
+        }
+      }
+    };
+    if (a.nout != 6) {
+      C w[3][E];
+      load_mu(w);
+      inverse_from(std::integral_constant<int, 6>(), w);
+      inverse_from(std::integral_constant<int, 7>(), w);
+      inverse_from(std::integral_constant<int, 8>(), w);
+    }
+    if (a.nout != 3) {
+      C v[3][E];
+      load_state(v);
+      inverse_from(std::integral_constant<int, 0>(), v);
+      inverse_from(std::integral_constant<int, 1>(), v);
+      inverse_from(std::integral_constant<int, 2>(), v);
+      inverse_from(std::integral_constant<int, 3>(), v);
+      inverse_from(std::integral_constant<int, 4>(), v);
+      inverse_from(std::integral_constant<int, 5>(), v);
+    }
   } else if constexpr (MODE == KX_NL_FWD) {  // spec_out = P F(u x omega) / N^3 (nonlinear term alone)
     const R inv_n3 = R(1) / (R(N) * R(N) * R(N));
     const C* win = a.in + (long long)run * 3 * g.sX + (long long)iyc * Hz + kz;
@@ -796,7 +902,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT) kx_reg_adj_kernel(const 
         for (int f = 0; f < 3; ++f) a.spec_out[soff + ((long long)f * M + ic) * M * Hz] = nv[f][q];
       }
     }
-  } else {  // KX_ADJ_FWD
+  } else {  // KX_ADJ_FWD, KX_ADJ_FWD_T
     const R inv_n3 = R(1) / (R(N) * R(N) * R(N));
     const C* win = a.in + (long long)run * 6 * g.sX + (long long)iyc * Hz + kz;
     C acc[3][E], z[E];
@@ -828,12 +934,82 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT) kx_reg_adj_kernel(const 
     add_curl(std::integral_constant<int, 0>());
     add_curl(std::integral_constant<int, 1>());
     add_curl(std::integral_constant<int, 2>());
+    // KX_ADJ_FWD_T: also fold g_s into the adjoint of the step input, lam (in vs):
+    //   s = 4: lam = E(h) (L + g4) (L in S);  s = 3, 2: lam += E(h/2) g_s;  s = 1: lam += g1
+    // and sum the stage's d(loss)/d(nu) terms (tape V, n1, n2, n3 in tp; w = 1 at kz = 0, else 2):
+    //   s = 4: <g4, -k^2 h E(h) V - k^2 h^2/2 E(h/2) n3>
+    //          + <L, -k^2 h E(h) V - k^2 h^2/6 (E(h) n1 + E(h/2) (n2 + n3))>
+    //   s = 3: <g3, -k^2 h/2 E(h/2) V>;   s = 2: <g2, -k^2 h/2 a2>, a2 = E(h/2) (V + h/2 n1)
+    // per mode in working precision, per CTA in FP64 (fixed order), into part[CTA]
+    const RunCoef cf = a.coef[run];
+    const R h = R(cf.dt);
+    const int st = a.stage;
+    double dsum = 0.0;
 #pragma unroll
     for (int q = 0; q < E; ++q) {
       const int ic = kcompact(t + P * q, N, K);
       if (zok && ic >= 0) {
+        R e1 = R(1), eh = R(1), mh = R(0), kk = R(0);
+        if constexpr (TAPE) {
+          const float kx = float(ksigned(ic, K));
+          kk = R(kx * kx + kyf * kyf + kzf * kzf);
+          const R lin = R(cf.nu * double(kk));
+          e1 = R(1) + rexpm1<R>(-lin * h);
+          mh = rexpm1<R>(R(-0.5) * lin * h);
+          eh = R(1) + mh;
+        }
+        R dn = R(0);
 #pragma unroll
-        for (int f = 0; f < 3; ++f) a.spec_out[soff + ((long long)f * M + ic) * M * Hz] = acc[f][q];
+        for (int f = 0; f < 3; ++f) {
+          const long long o = soff + ((long long)f * M + ic) * M * Hz;
+          const C gs = acc[f][q];
+          a.spec_out[o] = gs;
+          if constexpr (TAPE) {
+            C lam;
+            if (st == 4) {
+              const C l = a.S[o];
+              lam = mk<C>(e1 * (l.x + gs.x), e1 * (l.y + gs.y));
+            } else {
+              const R c = (st == 1) ? R(1) : eh;
+              lam = a.vs[o];
+              lam = mk<C>(lam.x + c * gs.x, lam.y + c * gs.y);
+            }
+            a.vs[o] = lam;
+            if (st >= 2) {
+              const C v = a.tp[0][o];
+              if (st == 4) {
+                const C y1 = a.tp[1][o], y2 = a.tp[2][o], y3 = a.tp[3][o], l = a.S[o];
+                const R b4x = -kk * h * e1 * v.x - kk * R(0.5) * h * h * eh * y3.x;
+                const R b4y = -kk * h * e1 * v.y - kk * R(0.5) * h * h * eh * y3.y;
+                const R bLx = -kk * h * e1 * v.x - kk * h * h / R(6) * (e1 * y1.x + eh * (y2.x + y3.x));
+                const R bLy = -kk * h * e1 * v.y - kk * h * h / R(6) * (e1 * y1.y + eh * (y2.y + y3.y));
+                dn += gs.x * b4x + gs.y * b4y + l.x * bLx + l.y * bLy;
+              } else if (st == 3) {
+                const R c3 = -kk * R(0.5) * h * eh;
+                dn += c3 * (gs.x * v.x + gs.y * v.y);
+              } else {
+                const C y1 = a.tp[1][o];
+                const R a2x = v.x + (mh * v.x + eh * R(0.5) * h * y1.x);
+                const R a2y = v.y + (mh * v.y + eh * R(0.5) * h * y1.y);
+                dn += -kk * R(0.5) * h * (gs.x * a2x + gs.y * a2y);
+              }
+            }
+          }
+        }
+        dsum += (kz == 0 ? 1.0 : 2.0) * double(dn);
+      }
+    }
+    if constexpr (TAPE) {
+      if (st >= 2) {  // CTA sum in a fixed order: warp tree, then the warps in turn
+        __shared__ double wsum[Sh::NT / 32];
+        for (int o = 16; o > 0; o >>= 1) dsum += __shfl_down_sync(0xffffffffu, dsum, o);
+        if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = dsum;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          double tot = 0.0;
+          for (int w = 0; w < Sh::NT / 32; ++w) tot += wsum[w];
+          a.part[blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z)] = tot;
+        }
       }
     }
   }

@@ -82,6 +82,14 @@ class Plan:
         return int(self.lib.tg_plan_scratch_bytes(self._h))
 
     @property
+    def state_bytes(self):
+        """Bytes of one state tensor (state_shape, complex)."""
+        n = 1
+        for d in self.state_shape:
+            n *= d
+        return n * (8 if self.precision == "f32" else 16)
+
+    @property
     def last_launch_count(self):
         return int(self.lib.tg_last_launch_count(self._h))
 
@@ -227,7 +235,14 @@ class Plan:
         return out
 
     def adjoint(self, state0, dt, nu, nsteps, checkpoint_every=0):
-        """(loss, grad_state, grad_nu) of loss = final enstrophy after nsteps steps."""
+        """(loss, grad_state, grad_nu) of loss = final enstrophy after nsteps steps.
+
+        checkpoint_every: > 0 checkpoints every that many steps and recomputes each
+        segment; 0 every ceil(sqrt(nsteps)) steps; "tape" (or -1) records every step's
+        stage data in pinned host memory in one forward sweep and recomputes nothing.
+        """
+        if checkpoint_every == "tape":
+            checkpoint_every = _abi.TG_ADJ_HOST_TAPE
         self._check_state(state0)
         grad = self.new_state()
         out = torch.zeros(2, dtype=torch.float64, device=self.device)  # grad_nu, loss

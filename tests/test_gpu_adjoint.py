@@ -106,3 +106,33 @@ def test_adjoint_128_fp32_finite_differences():
         ad = spectral_inner(p, grad, dd)
         rel.append(abs(ad - fd) / max(abs(fd), 1e-30))
     assert max(rel) < 3e-2, rel
+
+
+@pytest.mark.parametrize("N,nsteps", [(16, 5), (32, 9), (128, 6)])
+def test_host_tape_adjoint_matches_checkpointed(N, nsteps):
+    """The stage-tape adjoint (one forward sweep, stage data in pinned host memory, no
+    recomputation) and the checkpointed adjoint compute the same discrete gradient;
+    they differ only in FP32 rounding (stage states formed in another kernel)."""
+    p = _plan(N, "f32")
+    dt, nu = 2e-3, 1 / 400
+    s0 = p.initial_condition("taylor_green", seed=6, pert_amp=0.05, k0=3.0)
+    lc, gc, nc = p.adjoint(s0, dt, nu, nsteps, 2)
+    lt, gt, nt = p.adjoint(s0, dt, nu, nsteps, "tape")
+    assert float(lt) == pytest.approx(float(lc), rel=1e-6)
+    assert rel_l2(from_state(p, gt), from_state(p, gc)) < 2e-5
+    assert float(nt) == pytest.approx(float(nc), rel=1e-4)
+    # a second call reuses the plan's host tape
+    lt2, gt2, nt2 = p.adjoint(s0, dt, nu, nsteps, "tape")
+    assert float(lt2) == float(lt) and float(nt2) == float(nt)
+    assert bool((gt2 == gt).all())
+
+
+def test_host_tape_tracks_fp64_adjoint():
+    p32, p64 = _plan(32, "f32"), _plan(32, "f64")
+    s32 = p32.initial_condition("taylor_green", seed=4, pert_amp=0.05, k0=3.0)
+    s64 = p64.initial_condition("taylor_green", seed=4, pert_amp=0.05, k0=3.0)
+    l32, g32, n32 = p32.adjoint(s32, 2e-3, 1 / 400, 16, "tape")
+    l64, g64, n64 = p64.adjoint(s64, 2e-3, 1 / 400, 16, "tape")  # FP64: checkpointed instead
+    assert float(l32) == pytest.approx(float(l64), rel=1e-6)
+    assert rel_l2(from_state(p32, g32), from_state(p64, g64)) < 2e-5
+    assert float(n32) == pytest.approx(float(n64), rel=1e-4)
