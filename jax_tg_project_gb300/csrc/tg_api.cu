@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <new>
 #include <string>
 #include <vector>
@@ -1549,27 +1550,13 @@ struct Adjoint {
     TG_CUDA(cudaGraphInstantiate(&gx[k], gg[k], 0), "tape graph instantiate");
     return TG_OK;
   }
-  // one adjoint stage s of the step whose tape is tp = (V, n1, n2, n3); the stage's
-  // d(loss)/d(nu) partial sums go to part (one per CTA of the adjoint forward x pass)
-  int tape_stage(int s, const C* const tp[4], const C* L, C* LA, C* Gb, double* part, cudaEvent_t state_read) {
+  // y and z passes of one adjoint stage: a (x-pass layout, first three field slots of Y)
+  // and u, omega (X) -> Y (nine fields) -> in-place z (p, q) -> forward y -> X (six fields)
+  int tape_yz() {
     int rc;
     const Geo& g = p->g;
     C* X = static_cast<C*>(p->X);
     C* Y = static_cast<C*>(p->Y);
-    PassArgs<R> a = Ops<R>::base(p);
-    a.flags |= FLAG_TAPE;
-    a.stage = s;
-    for (int i = 0; i < 4; ++i) a.tp[i] = tp[i];
-    a.S = const_cast<C*>(L);
-    a.acc = Gb;
-    // u, omega of a_s -> X[0..5]; a = P mu_s -> the first three field slots of Y (read by the
-    // three-field y pass below before the six-field y pass overwrites them)
-    a.out = X;
-    a.out2 = Y;
-    a.nin = 6;
-    a.nout = 9;
-    if ((rc = Ops<R>::go(p, OP_KX_ADJ_LOAD, a, "kx adjoint load"))) return rc;
-    if (state_read) TG_CUDA(cudaEventRecord(state_read, p->st), "event record");
     PassArgs<R> b = Ops<R>::base(p);
     b.in = Y;  // x-pass layout (field stride sX)
     b.out = Y + 6 * g.sY;
@@ -1590,18 +1577,26 @@ struct Adjoint {
     b.in = Y;
     b.out = X;
     b.nin = b.nout = 6;
-    if ((rc = Ops<R>::go(p, OP_KY_FWD, b, "ky adjoint forward"))) return rc;
-    b = Ops<R>::base(p);
-    b.flags |= FLAG_TAPE;
-    b.stage = s;
-    for (int i = 0; i < 4; ++i) b.tp[i] = tp[i];
-    b.in = X;
-    b.S = const_cast<C*>(L);
-    b.vs = LA;
-    b.spec_out = Gb;
-    b.part = part;
-    b.nin = 6;
-    return Ops<R>::go(p, OP_KX_ADJ_FWD, b, "kx adjoint forward");
+    return Ops<R>::go(p, OP_KY_FWD, b, "ky adjoint forward");
+  }
+  // adjoint x pass of stage s: OP_KX_ADJ_LOAD (mu_s from L and g_{s+1} in G; a, u, omega)
+  // or OP_KX_ADJ_FWD (g_s into G unless null; lam accumulated in LA; nu partials into part)
+  int tape_x(int op, int s, const C* const tp[4], const C* L, C* LA, C* G, double* part) {
+    PassArgs<R> a = Ops<R>::base(p);
+    a.flags |= FLAG_TAPE;
+    a.stage = s;
+    for (int i = 0; i < 4; ++i) a.tp[i] = tp[i];
+    a.in = static_cast<C*>(p->X);
+    a.out = static_cast<C*>(p->X);
+    a.out2 = static_cast<C*>(p->Y);
+    a.S = const_cast<C*>(L);
+    a.acc = G;
+    a.spec_out = G;
+    a.vs = LA;
+    a.part = part;
+    a.nin = 6;
+    a.nout = 9;
+    return Ops<R>::go(p, op, a, "kx adjoint");
   }
   int run_tape(const void* state0, double dt, double nu, int nsteps, void* grad, double* grad_nu, double* loss) {
     int rc;
@@ -1680,44 +1675,60 @@ struct Adjoint {
     enstrophy_grad_kernel<R><<<blocks, 256, 0, st>>>(cur0, L, g);
     TG_CUDA(cudaMemsetAsync(dnu, 0, sizeof(double), st), "memset");
     if ((rc = launch_check("loss gradient"))) return rc;
-    // refill events: the tape buffers are reloaded once their last reader has run
+    // refill events: a tape buffer is reloaded as soon as its last reader has run
+    //   n3 (stage-4 nu terms), n2 (stage-3 state), n1 (stage-2 nu terms), V (stage-1 state)
     cudaEvent_t n3_free = event(), n2_free = event(), n1_free = event(), v_free[2] = {event(), event()};
     cudaEvent_t n3_ready = event(), n2_ready = event(), n1_ready = event(), v_ready[2] = {event(), event()};
     for (cudaEvent_t e : evs)
       if (!e) return fail(TG_E_CUDA, "tg_adjoint: event creation failed");
-    TG_CUDA(cudaEventRecord(v_free[0], st), "event record");  // the slots are free from here on
-    TG_CUDA(cudaEventRecord(v_free[1], st), "event record");
-    TG_CUDA(cudaEventRecord(n1_free, st), "event record");
-    TG_CUDA(cudaEventRecord(n2_free, st), "event record");
-    TG_CUDA(cudaEventRecord(n3_free, st), "event record");
-    auto fetch = [&](int j) -> int {
-      const C* src = host + (size_t)j * 4 * sN;
-      struct { C* dst; size_t off; cudaEvent_t free_, ready; } items[] = {
-          {N3, 3, n3_free, n3_ready}, {N2, 2, n2_free, n2_ready}, {N1, 1, n1_free, n1_ready},
-          {Vb[j & 1], 0, v_free[j & 1], v_ready[j & 1]}};
-      for (auto& it : items) {
-        TG_CUDA(cudaStreamWaitEvent(cs, it.free_, 0), "stream wait");
-        TG_CUDA(cudaMemcpyAsync(it.dst, src + it.off * sN, fbytes, cudaMemcpyHostToDevice, cs), "tape fetch");
-        TG_CUDA(cudaEventRecord(it.ready, cs), "event record");
-      }
+    for (cudaEvent_t e : {v_free[0], v_free[1], n1_free, n2_free, n3_free})  // the slots are free
+      TG_CUDA(cudaEventRecord(e, st), "event record");
+    auto fetch = [&](int j, C* dst, int item, cudaEvent_t free_, cudaEvent_t ready) -> int {
+      TG_CUDA(cudaStreamWaitEvent(cs, free_, 0), "stream wait");
+      TG_CUDA(cudaMemcpyAsync(dst, host + ((size_t)j * 4 + item) * sN, fbytes, cudaMemcpyHostToDevice, cs),
+              "tape fetch");
+      TG_CUDA(cudaEventRecord(ready, cs), "event record");
       return TG_OK;
     };
-    if ((rc = fetch(nsteps - 1))) return rc;
+    auto wait = [&](std::initializer_list<cudaEvent_t> es) -> int {
+      for (cudaEvent_t e : es) TG_CUDA(cudaStreamWaitEvent(st, e, 0), "stream wait");
+      return TG_OK;
+    };
     for (int j = nsteps - 1; j >= 0; --j) {
+      if (j == nsteps - 1) {
+        if ((rc = fetch(j, Vb[j & 1], 0, v_free[j & 1], v_ready[j & 1]))) return rc;
+        if ((rc = fetch(j, N3, 3, n3_free, n3_ready))) return rc;
+        if ((rc = fetch(j, N2, 2, n2_free, n2_ready))) return rc;
+        if ((rc = fetch(j, N1, 1, n1_free, n1_ready))) return rc;
+      }
+      if ((rc = wait({v_ready[j & 1], n1_ready, n2_ready, n3_ready}))) return rc;
+      // V of the next step goes to the other V buffer, free since stage 1 of step j + 1
+      if (j > 0 && (rc = fetch(j - 1, Vb[(j - 1) & 1], 0, v_free[(j - 1) & 1], v_ready[(j - 1) & 1])))
+        return rc;
       const C* tp[4] = {Vb[j & 1], N1, N2, N3};
-      for (cudaEvent_t e : {v_ready[j & 1], n1_ready, n2_ready, n3_ready})
-        TG_CUDA(cudaStreamWaitEvent(st, e, 0), "stream wait");
-      if ((rc = tape_stage(4, tp, L, LA, Gb, dpart, nullptr))) return rc;
-      TG_CUDA(cudaEventRecord(n3_free, st), "event record");
-      if ((rc = tape_stage(3, tp, L, LA, Gb, dpart + pslots, n2_free))) return rc;
-      if ((rc = tape_stage(2, tp, L, LA, Gb, dpart + 2 * pslots, nullptr))) return rc;
-      TG_CUDA(cudaEventRecord(n1_free, st), "event record");
-      if ((rc = tape_stage(1, tp, L, LA, Gb, nullptr, v_free[j & 1]))) return rc;
+      for (int s = 4; s >= 1; --s) {
+        if ((rc = tape_x(OP_KX_ADJ_LOAD, s, tp, L, LA, Gb, nullptr))) return rc;
+        if (s == 3) {
+          TG_CUDA(cudaEventRecord(n2_free, st), "event record");
+          if (j > 0 && (rc = fetch(j - 1, N2, 2, n2_free, n2_ready))) return rc;
+        }
+        if (s == 1) TG_CUDA(cudaEventRecord(v_free[j & 1], st), "event record");
+        if ((rc = tape_yz())) return rc;
+        double* part = (s >= 2) ? dpart + (size_t)(4 - s) * pslots : nullptr;
+        if ((rc = tape_x(OP_KX_ADJ_FWD, s, tp, L, LA, s > 1 ? Gb : nullptr, part))) return rc;
+        if (s == 4) {
+          TG_CUDA(cudaEventRecord(n3_free, st), "event record");
+          if (j > 0 && (rc = fetch(j - 1, N3, 3, n3_free, n3_ready))) return rc;
+        }
+        if (s == 2) {
+          TG_CUDA(cudaEventRecord(n1_free, st), "event record");
+          if (j > 0 && (rc = fetch(j - 1, N1, 1, n1_free, n1_ready))) return rc;
+        }
+      }
       accumulate_partials_wide<<<1, 256, 0, st>>>(dpart, (int)(3 * pslots), dnu);
       ++p->launches;
       if ((rc = launch_check("adjoint nu sum"))) return rc;
       std::swap(L, LA);
-      if (j > 0 && (rc = fetch(j - 1))) return rc;
     }
     TG_CUDA(cudaMemcpyAsync(grad, L, fbytes, cudaMemcpyDeviceToDevice, st), "grad copy");
     TG_CUDA(cudaMemcpyAsync(grad_nu, dnu, sizeof(double), cudaMemcpyDeviceToDevice, st), "grad_nu copy");

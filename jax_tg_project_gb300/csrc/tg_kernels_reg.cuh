@@ -727,9 +727,19 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT) kx_reg_kernel(const Pass
 }
 
 // ------------------------------------------------------------------ x pass, adjoint
-// KX_ADJ_LOAD: inverse-x of u, curl u of the state W (spec_in) and of a = P mu (mu in S)
-//              -> 9 fields (u 0..2, omega 3..5, a 6..8)
-// KX_ADJ_FWD:  forward-x of p (0..2), q (3..5) -> spec_out = F p + i k x F q (1/N^3 applied)
+// KX_ADJ_LOAD:   inverse-x of u, curl u of the state W (spec_in) and of a = P mu (mu in S)
+//                -> 9 fields (u 0..2, omega 3..5, a 6..8); nout = 3 / 6: only a / only u, omega
+// KX_ADJ_FWD:    forward-x of p (0..2), q (3..5) -> spec_out = F p + i k x F q (1/N^3 applied)
+// KX_NL_FWD:     spec_out = P F(u x omega) / N^3 (the nonlinear term alone)
+// Stage-tape forms (tp = the step tape V, n1, n2, n3; S = L, the adjoint of the step output):
+// KX_ADJ_LOAD_T: stage s = a.stage: mu_s = cl L + cg g_{s+1} (g_{s+1} in acc), a = P mu_s
+//                -> out2 (3 fields); u, curl u of the stage state a_s (from V, n_{s-1}) -> out
+// KX_ADJ_FWD_T:  stage s: g_s as KX_ADJ_FWD (-> spec_out unless null); lam (vs) accumulated:
+//                s = 4: lam = E(h) (L + g4);  s = 3, 2: lam += E(h/2) g_s;  s = 1: lam += g1;
+//                d(loss)/d(nu) terms of the stage (w = 1 at kz = 0, else 2) -> part[CTA]:
+//                s = 4: <g4, -k^2 h E(h) V - k^2 h^2/2 E(h/2) n3>
+//                       + <L, -k^2 h E(h) V - k^2 h^2/6 (E(h) n1 + E(h/2) (n2 + n3))>
+//                s = 3: <g3, -k^2 h/2 E(h/2) V>;  s = 2: <g2, -k^2 h/2 a2>, a2 = E(h/2)(V + h/2 n1)
 template <typename R, int N, int MODE>
 __global__ void __launch_bounds__(KxRegShape<R, N>::NT, 2) kx_reg_adj_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
@@ -737,6 +747,9 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, 2) kx_reg_adj_kernel(con
   using Plan = typename Sh::Plan;
   constexpr int P = Sh::P, E = Sh::E, QW = Sh::QW, GT = Sh::GT, CS = Sh::CS;
   constexpr int NBL = N / (Plan::template radix<Plan::NPASS - 1>() * P);
+  constexpr bool TAPE = (MODE == KX_ADJ_LOAD_T || MODE == KX_ADJ_FWD_T);
+  constexpr bool HAS_FWD = (MODE == KX_ADJ_FWD || MODE == KX_ADJ_FWD_T);
+  constexpr bool HAS_INV = (MODE == KX_ADJ_LOAD || MODE == KX_ADJ_LOAD_T);
   const Geo g = a.g;
   const int K = g.K, M = g.M, Hz = g.Hz;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -751,6 +764,9 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, 2) kx_reg_adj_kernel(con
   __syncthreads();
   const float kyf = float(ksigned(iyc, K)), kzf = float(kz);
   const long long soff = (long long)run * 3 * g.sS + (long long)iyc * Hz + kz;
+  const RunCoef cf = a.coef[run];
+  const R h = R(cf.dt);
+  const int st = a.stage;
   auto run_fft = [&](auto& src, auto& dst, auto dir_tag) {
     constexpr int DIR = decltype(dir_tag)::value;
     if constexpr (GT > 32) {
@@ -763,126 +779,24 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, 2) kx_reg_adj_kernel(con
   };
   using Fwd = std::integral_constant<int, -1>;
   using Inv = std::integral_constant<int, +1>;
-  constexpr bool TAPE = (MODE == KX_ADJ_LOAD_T || MODE == KX_ADJ_FWD_T);
-  if constexpr (MODE == KX_ADJ_LOAD || MODE == KX_ADJ_LOAD_T) {
-    // a = P mu first (its three transforms retire w), then u, curl u of the state:
-    // only one three-field array is live at a time.  nout = 9 writes both into fields
-    // 0..8 (u, omega, a); nout = 3 only a (into fields 0..2), nout = 6 only u, omega.
-    // KX_ADJ_LOAD_T: the stage state and mu are formed here from the step tape:
-    //   state a_s from V (tp[0]) and n_{s-1} (tp[s-1]) by the Lawson stage formula,
-    //   mu_s = cl L + cg g_{s+1} (L in S, g_{s+1} in acc) with the adjoint seeds of the tableau.
-    constexpr bool tape = TAPE;
-    const RunCoef cf = a.coef[run];
-    const R h = R(cf.dt);
-    const int st = a.stage;
-    C* xo = a.out + (long long)run * a.nout * g.sX + (long long)iyc * Hz + kz;
-    const int gi0 = (a.nout == 3) ? 6 : 0;  // output field of GI = gi0 + slot
-    // KX_ADJ_LOAD_T with nout = 9: u, omega into out (6 fields), a into out2 (3 fields)
-    C* xa = (TAPE && a.nout == 9) ? a.out2 + (long long)iyc * Hz + kz - 6 * g.sX : xo - gi0 * g.sX;
-    auto inverse_from = [&](auto gi_tag, auto* arr) {
-      constexpr int GI = decltype(gi_tag)::value;
-      auto src = [&](int k, int q) -> C {
-        const int ic = kcompact(k, N, K);
-        if (ic < 0) return czero<C>();
-        if constexpr (GI < 6) return uw_field<GI>(arr, q, float(ksigned(ic, K)), kyf, kzf);
-        else return arr[GI - 6][q];
-      };
-      C* xg = (GI >= 6) ? xa + GI * g.sX : xo + (GI - gi0) * g.sX;
-      auto dst = [&](int, int, int xx, C val) {
-        if (zok) xg[(long long)xx * M * Hz] = val;
-      };
-      run_fft(src, dst, Inv());
-    };
-    // Lawson factors expm1(-nu k^2 h), expm1(-nu k^2 h / 2) of mode (ic, iyc, kz)
-    auto factors = [&](int ic, R& m1, R& mh) {
-      const float kx = float(ksigned(ic, K));
-      const R lin = R(cf.nu * double(kx * kx + kyf * kyf + kzf * kzf));
-      m1 = rexpm1<R>(-lin * h);
-      mh = rexpm1<R>(R(-0.5) * lin * h);
-    };
-    // mu (projected) into w: plain S, or the tape seeds cl L + cg g
-    auto load_mu = [&](auto* w) {
-#pragma unroll
-      for (int q = 0; q < E; ++q) {
-        const int ic = kcompact(t + P * q, N, K);
-        const bool ok = zok && ic >= 0;
-        R cl = R(1), cg = R(0);
-        if (tape && ok) {
-          R m1, mh;
-          factors(ic, m1, mh);
-          const R e1 = R(1) + m1, eh = R(1) + mh;
-          if (st == 4) { cl = h / R(6); }
-          else if (st == 3) { cl = h / R(3) * eh; cg = h * eh; }
-          else if (st == 2) { cl = h / R(3) * eh; cg = R(0.5) * h; }
-          else { cl = h / R(6) * e1; cg = R(0.5) * h * eh; }
-        }
-#pragma unroll
-        for (int f = 0; f < 3; ++f) {
-          const long long o = soff + ((long long)f * M + (ok ? ic : 0)) * M * Hz;
-          C m = czero<C>();
-          if (ok) {
-            const C l = a.S[o];
-            m = mk<C>(cl * l.x, cl * l.y);
-            if (tape && st != 4) {
-              const C gp = a.acc[o];
-              m = mk<C>(m.x + cg * gp.x, m.y + cg * gp.y);
-            }
-          }
-          w[f][q] = m;
-        }
-        if (ok) {
-          const float kx = float(ksigned(ic, K));
-          leray(w[0][q], w[1][q], w[2][q], kx, kyf, kzf, kx * kx + kyf * kyf + kzf * kzf);
-        }
-      }
-    };
-    // the state whose u, curl u are transformed: spec_in, or the tape's stage state
-    auto load_state = [&](auto* v) {
-#pragma unroll
-      for (int q = 0; q < E; ++q) {
-        const int ic = kcompact(t + P * q, N, K);
-        const bool ok = zok && ic >= 0;
-        R m1 = R(0), mh = R(0);
-        if (tape && ok && st > 1) factors(ic, m1, mh);
-        const R eh = R(1) + mh;
-#pragma unroll
-        for (int f = 0; f < 3; ++f) {
-          const long long o = soff + ((long long)f * M + (ok ? ic : 0)) * M * Hz;
-          C x = czero<C>();
-          if (ok) {
-            x = tape ? a.tp[0][o] : a.spec_in[o];
-            if (tape && st > 1) {
-              const C nn = a.tp[st - 1][o];
-              R dx, dy;
-              if (st == 2) { dx = mh * x.x + eh * R(0.5) * h * nn.x; dy = mh * x.y + eh * R(0.5) * h * nn.y; }
-              else if (st == 3) { dx = mh * x.x + R(0.5) * h * nn.x; dy = mh * x.y + R(0.5) * h * nn.y; }
-              else { dx = m1 * x.x + h * eh * nn.x; dy = m1 * x.y + h * eh * nn.y; }
-              x = mk<C>(x.x + dx, x.y + dy);
-            }
-          }
-          v[f][q] = x;
-        }
-      }
-    };
-    if (a.nout != 6) {
-      C w[3][E];
-      load_mu(w);
-      inverse_from(std::integral_constant<int, 6>(), w);
-      inverse_from(std::integral_constant<int, 7>(), w);
-      inverse_from(std::integral_constant<int, 8>(), w);
-    }
-    if (a.nout != 3) {
-      C v[3][E];
-      load_state(v);
-      inverse_from(std::integral_constant<int, 0>(), v);
-      inverse_from(std::integral_constant<int, 1>(), v);
-      inverse_from(std::integral_constant<int, 2>(), v);
-      inverse_from(std::integral_constant<int, 3>(), v);
-      inverse_from(std::integral_constant<int, 4>(), v);
-      inverse_from(std::integral_constant<int, 5>(), v);
-    }
-  } else if constexpr (MODE == KX_NL_FWD) {  // spec_out = P F(u x omega) / N^3 (nonlinear term alone)
-    const R inv_n3 = R(1) / (R(N) * R(N) * R(N));
+  const R inv_n3 = R(1) / (R(N) * R(N) * R(N));
+  // k^2 and the Lawson factors expm1(-nu k^2 h), expm1(-nu k^2 h / 2) of mode (ic, iyc, kz)
+  auto factors = [&](int ic, R& kk, R& m1, R& mh) {
+    const float kx = float(ksigned(ic, K));
+    kk = R(kx * kx + kyf * kyf + kzf * kzf);
+    const R lin = R(cf.nu * double(kk));
+    m1 = rexpm1<R>(-lin * h);
+    mh = rexpm1<R>(R(-0.5) * lin * h);
+  };
+  // adjoint seeds of the stage nonlinear terms: mu_s = cl L + cg g_{s+1}
+  auto seeds = [&](int s, R e1, R eh, R& cl, R& cg) {
+    if (s == 4) { cl = h / R(6); cg = R(0); }
+    else if (s == 3) { cl = h / R(3) * eh; cg = h * eh; }
+    else if (s == 2) { cl = h / R(3) * eh; cg = R(0.5) * h; }
+    else { cl = h / R(6) * e1; cg = R(0.5) * h * eh; }
+  };
+
+  if constexpr (MODE == KX_NL_FWD) {  // spec_out = P F(u x omega) / N^3 (nonlinear term alone)
     const C* win = a.in + (long long)run * 3 * g.sX + (long long)iyc * Hz + kz;
     C nv[3][E];
 #pragma unroll
@@ -902,10 +816,13 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, 2) kx_reg_adj_kernel(con
         for (int f = 0; f < 3; ++f) a.spec_out[soff + ((long long)f * M + ic) * M * Hz] = nv[f][q];
       }
     }
-  } else {  // KX_ADJ_FWD, KX_ADJ_FWD_T
-    const R inv_n3 = R(1) / (R(N) * R(N) * R(N));
+    return;
+  }
+
+  C acc[3][E];  // g_s (forward part) or mu (projected, load part)
+  if constexpr (HAS_FWD) {
+    C z[E];
     const C* win = a.in + (long long)run * 6 * g.sX + (long long)iyc * Hz + kz;
-    C acc[3][E], z[E];
     auto fwd_to = [&](int f, auto* dstarr) {
       const C* wf = win + f * g.sX;
       auto src = [&](int xx, int) -> C { return zok ? wf[(long long)xx * M * Hz] : czero<C>(); };
@@ -934,40 +851,28 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, 2) kx_reg_adj_kernel(con
     add_curl(std::integral_constant<int, 0>());
     add_curl(std::integral_constant<int, 1>());
     add_curl(std::integral_constant<int, 2>());
-    // KX_ADJ_FWD_T: also fold g_s into the adjoint of the step input, lam (in vs):
-    //   s = 4: lam = E(h) (L + g4) (L in S);  s = 3, 2: lam += E(h/2) g_s;  s = 1: lam += g1
-    // and sum the stage's d(loss)/d(nu) terms (tape V, n1, n2, n3 in tp; w = 1 at kz = 0, else 2):
-    //   s = 4: <g4, -k^2 h E(h) V - k^2 h^2/2 E(h/2) n3>
-    //          + <L, -k^2 h E(h) V - k^2 h^2/6 (E(h) n1 + E(h/2) (n2 + n3))>
-    //   s = 3: <g3, -k^2 h/2 E(h/2) V>;   s = 2: <g2, -k^2 h/2 a2>, a2 = E(h/2) (V + h/2 n1)
-    // per mode in working precision, per CTA in FP64 (fixed order), into part[CTA]
-    const RunCoef cf = a.coef[run];
-    const R h = R(cf.dt);
-    const int st = a.stage;
     double dsum = 0.0;
 #pragma unroll
     for (int q = 0; q < E; ++q) {
       const int ic = kcompact(t + P * q, N, K);
       if (zok && ic >= 0) {
-        R e1 = R(1), eh = R(1), mh = R(0), kk = R(0);
-        if constexpr (TAPE) {
-          const float kx = float(ksigned(ic, K));
-          kk = R(kx * kx + kyf * kyf + kzf * kzf);
-          const R lin = R(cf.nu * double(kk));
-          e1 = R(1) + rexpm1<R>(-lin * h);
-          mh = rexpm1<R>(R(-0.5) * lin * h);
-          eh = R(1) + mh;
-        }
-        R dn = R(0);
+        if constexpr (!TAPE) {
 #pragma unroll
-        for (int f = 0; f < 3; ++f) {
-          const long long o = soff + ((long long)f * M + ic) * M * Hz;
-          const C gs = acc[f][q];
-          a.spec_out[o] = gs;
-          if constexpr (TAPE) {
+          for (int f = 0; f < 3; ++f) a.spec_out[soff + ((long long)f * M + ic) * M * Hz] = acc[f][q];
+        } else {
+          R kk, m1, mh;
+          factors(ic, kk, m1, mh);
+          const R e1 = R(1) + m1, eh = R(1) + mh;
+          R dn = R(0);
+#pragma unroll
+          for (int f = 0; f < 3; ++f) {
+            const long long o = soff + ((long long)f * M + ic) * M * Hz;
+            const C gs = acc[f][q];
+            if (a.spec_out != nullptr) a.spec_out[o] = gs;
             C lam;
+            C l = czero<C>();
+            if (st >= 2) l = a.S[o];
             if (st == 4) {
-              const C l = a.S[o];
               lam = mk<C>(e1 * (l.x + gs.x), e1 * (l.y + gs.y));
             } else {
               const R c = (st == 1) ? R(1) : eh;
@@ -978,7 +883,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, 2) kx_reg_adj_kernel(con
             if (st >= 2) {
               const C v = a.tp[0][o];
               if (st == 4) {
-                const C y1 = a.tp[1][o], y2 = a.tp[2][o], y3 = a.tp[3][o], l = a.S[o];
+                const C y1 = a.tp[1][o], y2 = a.tp[2][o], y3 = a.tp[3][o];
                 const R b4x = -kk * h * e1 * v.x - kk * R(0.5) * h * h * eh * y3.x;
                 const R b4y = -kk * h * e1 * v.y - kk * R(0.5) * h * h * eh * y3.y;
                 const R bLx = -kk * h * e1 * v.x - kk * h * h / R(6) * (e1 * y1.x + eh * (y2.x + y3.x));
@@ -995,12 +900,12 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, 2) kx_reg_adj_kernel(con
               }
             }
           }
+          dsum += (kz == 0 ? 1.0 : 2.0) * double(dn);
         }
-        dsum += (kz == 0 ? 1.0 : 2.0) * double(dn);
       }
     }
     if constexpr (TAPE) {
-      if (st >= 2) {  // CTA sum in a fixed order: warp tree, then the warps in turn
+      if (st >= 2 && a.part != nullptr) {  // CTA sum in a fixed order: warp tree, then the warps
         __shared__ double wsum[Sh::NT / 32];
         for (int o = 16; o > 0; o >>= 1) dsum += __shfl_down_sync(0xffffffffu, dsum, o);
         if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = dsum;
@@ -1011,6 +916,102 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, 2) kx_reg_adj_kernel(con
           a.part[blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z)] = tot;
         }
       }
+    }
+  }
+
+  if constexpr (HAS_INV) {
+    // a = P mu first (its three transforms retire the mu registers), then u, curl u of the
+    // state: one three-field array live at a time.  nout = 9 writes u, omega into out and a
+    // into out2 (tape forms) or into out's fields 6..8; nout = 3 only a, nout = 6 only u, omega.
+    const int sl = st;  // load stage
+    const C* const* tape = a.tp;
+    C* xo = a.out + (long long)run * a.nout * g.sX + (long long)iyc * Hz + kz;
+    const int gi0 = (a.nout == 3) ? 6 : 0;  // output field of GI = gi0 + slot
+    C* xa = (TAPE && a.nout == 9) ? a.out2 + (long long)iyc * Hz + kz - 6 * g.sX : xo - gi0 * g.sX;
+    auto inverse_from = [&](auto gi_tag, auto* arr) {
+      constexpr int GI = decltype(gi_tag)::value;
+      auto src = [&](int k, int q) -> C {
+        const int ic = kcompact(k, N, K);
+        if (ic < 0) return czero<C>();
+        if constexpr (GI < 6) return uw_field<GI>(arr, q, float(ksigned(ic, K)), kyf, kzf);
+        else return arr[GI - 6][q];
+      };
+      C* xg = (GI >= 6) ? xa + GI * g.sX : xo + (GI - gi0) * g.sX;
+      auto dst = [&](int, int, int xx, C val) {
+        if (zok) xg[(long long)xx * M * Hz] = val;
+      };
+      run_fft(src, dst, Inv());
+    };
+    {  // mu (projected) into acc: plain S, or the tape seeds
+#pragma unroll
+      for (int q = 0; q < E; ++q) {
+        const int ic = kcompact(t + P * q, N, K);
+        const bool ok = zok && ic >= 0;
+        R cl = R(1), cg = R(0);
+        if (TAPE && ok) {
+          R kk, m1, mh;
+          factors(ic, kk, m1, mh);
+          seeds(sl, R(1) + m1, R(1) + mh, cl, cg);
+        }
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+          const long long o = soff + ((long long)f * M + (ok ? ic : 0)) * M * Hz;
+          C m = czero<C>();
+          if (ok && a.nout != 6) {
+            const C l = a.S[o];
+            m = mk<C>(cl * l.x, cl * l.y);
+            if (TAPE && sl != 4) {
+              const C gp = a.acc[o];
+              m = mk<C>(m.x + cg * gp.x, m.y + cg * gp.y);
+            }
+          }
+          acc[f][q] = m;
+        }
+        if (ok && a.nout != 6) {
+          const float kx = float(ksigned(ic, K));
+          leray(acc[0][q], acc[1][q], acc[2][q], kx, kyf, kzf, kx * kx + kyf * kyf + kzf * kzf);
+        }
+      }
+    }
+    if (a.nout != 6) {
+      inverse_from(std::integral_constant<int, 6>(), acc);
+      inverse_from(std::integral_constant<int, 7>(), acc);
+      inverse_from(std::integral_constant<int, 8>(), acc);
+    }
+    if (a.nout != 3) {
+      // the state whose u, curl u are transformed: spec_in, or the tape's stage state a_sl
+      C v[3][E];
+#pragma unroll
+      for (int q = 0; q < E; ++q) {
+        const int ic = kcompact(t + P * q, N, K);
+        const bool ok = zok && ic >= 0;
+        R kk = R(0), m1 = R(0), mh = R(0);
+        if (TAPE && ok && sl > 1) factors(ic, kk, m1, mh);
+        const R eh = R(1) + mh;
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+          const long long o = soff + ((long long)f * M + (ok ? ic : 0)) * M * Hz;
+          C x = czero<C>();
+          if (ok) {
+            x = TAPE ? tape[0][o] : a.spec_in[o];
+            if (TAPE && sl > 1) {
+              const C nn = tape[sl - 1][o];
+              R dx, dy;
+              if (sl == 2) { dx = mh * x.x + eh * R(0.5) * h * nn.x; dy = mh * x.y + eh * R(0.5) * h * nn.y; }
+              else if (sl == 3) { dx = mh * x.x + R(0.5) * h * nn.x; dy = mh * x.y + R(0.5) * h * nn.y; }
+              else { dx = m1 * x.x + h * eh * nn.x; dy = m1 * x.y + h * eh * nn.y; }
+              x = mk<C>(x.x + dx, x.y + dy);
+            }
+          }
+          v[f][q] = x;
+        }
+      }
+      inverse_from(std::integral_constant<int, 0>(), v);
+      inverse_from(std::integral_constant<int, 1>(), v);
+      inverse_from(std::integral_constant<int, 2>(), v);
+      inverse_from(std::integral_constant<int, 3>(), v);
+      inverse_from(std::integral_constant<int, 4>(), v);
+      inverse_from(std::integral_constant<int, 5>(), v);
     }
   }
 }
