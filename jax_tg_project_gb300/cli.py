@@ -10,7 +10,8 @@ Subcommands mirror the reference's entry points:
 
 Extensions: --precision f32|f64, --save PATH (final state + series to .npz), --resume PATH
 (start from a saved state, continuing its step count and time), --spectrum (print E(k) at the
-end).  Plots are not produced (--no-plots is accepted for compatibility).
+end), --plot-dir DIR.  Like the reference CLIs, the hydro and mhd subcommands write the slice
+and diagnostics PNGs (headless, plots.py) unless --no-plots is given.
 """
 from __future__ import annotations
 
@@ -24,7 +25,7 @@ import numpy as np
 
 
 def _run(physics, n, dt, nu, eta, total_time, save_every_time, precision, save, resume,
-         spectrum, b_amp, lorentz_sign, out=None):
+         spectrum, b_amp, lorentz_sign, out=None, plots=False, plot_dir="."):
     import torch
 
     out = out or sys.stdout
@@ -74,6 +75,12 @@ def _run(physics, n, dt, nu, eta, total_time, save_every_time, precision, save, 
     if spectrum:
         e = plan.energy_spectrum(state).cpu().numpy()[0]
         print("E(k): " + json.dumps([float(x) for x in np.atleast_2d(e)[0]]), file=out)
+    if plots:
+        from .plots import save_plots
+        r = save_plots(plan, state, times, series.cpu().numpy(), kind=physics, directory=plot_dir)
+        lo, hi = min(x[0] for x in r["slice_ranges"]), max(x[1] for x in r["slice_ranges"])
+        print(f"Saved: {r['slice']} (values {lo:.4e} .. {hi:.4e})", file=out)
+        print(f"Saved: {r['diagnostics']}", file=out)
     if save:
         plan.save(save, state, step=step0 + steps, time=t0 + steps * dt, nu=nu, eta=eta, dt=dt,
                   series=series.cpu().numpy(), series_keys=np.array(DIAG_KEYS), times=np.array(times))
@@ -92,6 +99,7 @@ def main(argv=None):
         p.add_argument("--total-time", type=float, default=total)
         p.add_argument("--save-every-time", type=float, default=save_every)
         p.add_argument("--no-plots", action="store_true")
+        p.add_argument("--plot-dir", default=".")
         p.add_argument("--precision", choices=("f32", "f64"), default="f32")
         p.add_argument("--save", default=None)
         p.add_argument("--resume", default=None)
@@ -124,14 +132,15 @@ def main(argv=None):
         cfg = TaylorGreenConfig(a.n, a.dt, a.reynolds, a.total_time, a.save_every_time)
         nu = cfg.viscosity if a.nu is None else a.nu
         return _run("hydro", cfg.n, cfg.dt, nu, 0.0, cfg.total_time, cfg.save_every_time,
-                    a.precision, a.save, a.resume, a.spectrum, 0.0, 1.0)
+                    a.precision, a.save, a.resume, a.spectrum, 0.0, 1.0, plots=not a.no_plots,
+                    plot_dir=a.plot_dir)
     cfg = TaylorGreenMhdConfig(n=a.n, dt=a.dt, reynolds=a.reynolds,
                                magnetic_reynolds=a.magnetic_reynolds,
                                magnetic_amplitude=a.magnetic_amplitude, total_time=a.total_time,
                                save_every_time=a.save_every_time)
     return _run("mhd", cfg.n, cfg.dt, cfg.viscosity, cfg.resistivity, cfg.total_time,
                 cfg.save_every_time, a.precision, a.save, a.resume, a.spectrum,
-                cfg.magnetic_amplitude, a.lorentz_sign)
+                cfg.magnetic_amplitude, a.lorentz_sign, plots=not a.no_plots, plot_dir=a.plot_dir)
 
 
 if __name__ == "__main__":

@@ -101,11 +101,13 @@ _DIAG_ATTRS = ("times", "kinetic_energies", "magnetic_energies", "total_energies
 
 
 def run_simulation(n=128, dt=0.005, reynolds=1000.0, magnetic_reynolds=1000.0,
-                   magnetic_amplitude=0.5, total_time=1.0, save_every_time=0.05, make_plots=True,
-                   lorentz_sign=1.0, initial="reference", verbose=True):
+                   magnetic_amplitude=0.5, total_time=1.0, save_every_time=0.05, make_plots=False,
+                   lorentz_sign=1.0, initial="reference", verbose=True, plot_dir="."):
     """TaylorGreenMhdSimulation.run (cuda/taylor_green_mhd.py:72-99): returns
-    (u, b, diagnostics) with the MhdDiagnostics list attributes.  Plots are not
-    produced.  ``initial='equal_energy'`` selects the equal-energy b field."""
+    (u, b, diagnostics) with the MhdDiagnostics list attributes.  ``make_plots`` writes
+    taylor_green_mhd_slice.png / taylor_green_mhd_diagnostics.png
+    (cuda/taylor_green_mhd/plotting.py:9-48) into ``plot_dir``.
+    ``initial='equal_energy'`` selects the equal-energy b field."""
     cfg = TaylorGreenMhdConfig(n=n, dt=dt, reynolds=reynolds, magnetic_reynolds=magnetic_reynolds,
                                magnetic_amplitude=magnetic_amplitude, total_time=total_time,
                                save_every_time=save_every_time)
@@ -141,5 +143,8 @@ def run_simulation(n=128, dt=0.005, reynolds=1000.0, magnetic_reynolds=1000.0,
         print(f"Magnetic Reynolds number: Rm = {cfg.magnetic_reynolds:.1f}")
         print(f"Simulated time: {cfg.total_time:.3f} ({cfg.steps} steps) in {elapsed:.3f} s")
         print(f"Max divergence u: {max(d.divergence_u_max):.3e}, B: {max(d.divergence_b_max):.3e}")
+    if make_plots:
+        from .plots import save_plots
+        save_plots(p, s, times, series.cpu().numpy(), kind="mhd", directory=plot_dir)
     f = p.inverse(s)[0]
     return f[:3], f[3:], d

@@ -75,9 +75,10 @@ def enstrophy(velocity, kx, ky, kz):
 
 
 def run_simulation(n=128, dt=0.005, reynolds=1000.0, total_time=1.0, save_every_time=0.05,
-                   verbose=True):
+                   verbose=True, make_plots=False, plot_dir="."):
     """TaylorGreenSimulation.run (cuda/taylor_green_cuda.py:63-69): returns
-    (u, times, energies, enstrophies)."""
+    (u, times, energies, enstrophies); ``make_plots`` writes taylor_green_cuda_slice.png and
+    taylor_green_cuda_diagnostics.png (cuda/taylor_green_cuda/plotting.py:7-31)."""
     cfg = TaylorGreenConfig(n, dt, reynolds, total_time, save_every_time)
     p = rt.get_plan(cfg.n)
     s = p.initial_condition("taylor_green")
@@ -99,4 +100,7 @@ def run_simulation(n=128, dt=0.005, reynolds=1000.0, total_time=1.0, save_every_
         print(f"Reynolds number: {cfg.reynolds:.1f}")
         print(f"Simulated time: {cfg.total_time:.3f} ({cfg.steps} steps) in {elapsed:.3f} s")
         print(f"Energy trace: {energies[0]:.6f} -> {energies[-1]:.6f}")
+    if make_plots:
+        from .plots import save_plots
+        save_plots(p, s, times, series.cpu().numpy(), kind="hydro", directory=plot_dir)
     return p.inverse(s)[0], times, energies, enstrophies

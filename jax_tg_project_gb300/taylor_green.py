@@ -125,12 +125,14 @@ def advance_one_step(u, dt, nu, kx, ky, kz, dealias_mask):
 
 
 def run_simulation(N=16, dt=0.005, nu=None, reynolds=None, total_time=0.5, save_every_time=0.05,
-                   cfl=0.5, return_diagnostics=False, precision=None, verbose=True, u0=None):
-    """Decaying Taylor-Green run (jax/taylor_green_jax.py:204-317) without plots.
+                   cfl=0.5, return_diagnostics=False, precision=None, verbose=True, u0=None,
+                   make_plots=False, plot_dir="."):
+    """Decaying Taylor-Green run (jax/taylor_green_jax.py:204-317).
 
     Returns (u, energies) or (u, energies, diagnostics) with the reference's keys
     time, energy, divergence_max, enstrophy and dissipation.  ``u0`` optionally
-    replaces the Taylor-Green initial field.
+    replaces the Taylor-Green initial field.  ``make_plots`` writes the reference's
+    taylor_green_slice.png / taylor_green_diagnostics.png into ``plot_dir``.
     """
     if N < 4 or total_time <= 0.0 or save_every_time <= 0.0:
         raise ValueError("N must be at least 4, total_time and save_every_time must be positive")
@@ -174,6 +176,12 @@ def run_simulation(N=16, dt=0.005, nu=None, reynolds=None, total_time=0.5, save_
         print(f"Simulated time: {total_time:.3f} ({n_steps} steps) in {elapsed:.3f} s")
         print(f"Energy trace: {energies[0]:.6f} -> {energies[-1]:.6f}")
         print(f"Max divergence: {max(diag['divergence_max']):.3e}")
+    if make_plots:
+        from .plots import save_plots
+        out = save_plots(p, s, times, series.cpu().numpy(), kind="jax", directory=plot_dir)
+        if verbose:
+            print(f"Saved: {out['slice']}")
+            print(f"Saved: {out['diagnostics']}")
     u = p.inverse(s)[0]
     if return_diagnostics:
         return u, energies, diag
