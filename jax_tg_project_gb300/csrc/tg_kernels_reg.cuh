@@ -554,6 +554,8 @@ struct KxRegShape {
   static constexpr int TARGET = (P >= 16) ? 256 : 128;  // threads per CTA
   static constexpr int NG = (GT >= TARGET) ? 1 : TARGET / GT;
   static constexpr int NT = NG * GT;
+  // resident CTAs per SM the registers must allow (E = 12 at N = 96 needs ~168 registers)
+  static constexpr int MINB = (NT >= 256) ? 2 : ((E > 8) ? 3 : 4);
   static constexpr int PSH = 3;
   static constexpr int CS = ColLayout<N, PSH, 4>::CS;
   static constexpr int MMAX = 2 * (N / 3) + 1;
@@ -576,7 +578,7 @@ __device__ __forceinline__ auto uw_field(const A& v, int q, float kx, float ky, 
 }
 
 template <typename R, int N, int MODE>
-__global__ void __launch_bounds__(KxRegShape<R, N>::NT) kx_reg_kernel(const PassArgs<R> a) {
+__global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) kx_reg_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Sh = KxRegShape<R, N>;
   using Plan = typename Sh::Plan;
@@ -703,27 +705,55 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT) kx_reg_kernel(const Pass
     }
   }
 
-  // inverse-x of u and curl u straight from the registers
+  // inverse-x of u and curl u straight from the registers.  At N >= 128 the six transforms
+  // share one FFT body (a loop over a uniform field index; the values of this thread's modes
+  // are formed first by a switch whose cases index the registers at compile time), which
+  // keeps the kernel's code small enough for the instruction cache; smaller transforms are
+  // unrolled (the loop would raise their register count and lower occupancy).
   C* xo = a.out + (long long)run * 6 * g.sX + (long long)iyc * Hz + kz;
-  auto inverse = [&](auto gi_tag) {
+  auto values = [&](auto gi_tag, C* in) {
     constexpr int GI = decltype(gi_tag)::value;
-    auto src = [&](int k, int q) -> C {
-      const int ic = kcompact(k, N, K);
-      if (ic < 0) return czero<C>();
-      return uw_field<GI>(v, q, float(ksigned(ic, K)), kyf, kzf);
-    };
-    C* xg = xo + GI * g.sX;
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      const int ic = kcompact(t + P * q, N, K);
+      in[q] = (ic < 0) ? czero<C>() : uw_field<GI>(v, q, float(ksigned(ic, K)), kyf, kzf);
+    }
+  };
+  auto inverse_of = [&](const C* in, int gi) {
+    auto src = [&](int, int q) -> C { return in[q]; };
+    C* xg = xo + gi * g.sX;
     auto dst = [&](int, int, int x, C val) {
       if (zok) xg[(long long)x * M * Hz] = val;
     };
     run_fft(src, dst, Inv());
   };
-  inverse(std::integral_constant<int, 0>());
-  inverse(std::integral_constant<int, 1>());
-  inverse(std::integral_constant<int, 2>());
-  inverse(std::integral_constant<int, 3>());
-  inverse(std::integral_constant<int, 4>());
-  inverse(std::integral_constant<int, 5>());
+  if constexpr (N >= 128) {
+#pragma unroll 1
+    for (int gi = 0; gi < 6; ++gi) {
+      C in[E];
+      switch (gi) {
+        case 0: values(std::integral_constant<int, 0>(), in); break;
+        case 1: values(std::integral_constant<int, 1>(), in); break;
+        case 2: values(std::integral_constant<int, 2>(), in); break;
+        case 3: values(std::integral_constant<int, 3>(), in); break;
+        case 4: values(std::integral_constant<int, 4>(), in); break;
+        default: values(std::integral_constant<int, 5>(), in); break;
+      }
+      inverse_of(in, gi);
+    }
+  } else {
+    auto inverse = [&](auto gi_tag) {
+      C in[E];
+      values(gi_tag, in);
+      inverse_of(in, decltype(gi_tag)::value);
+    };
+    inverse(std::integral_constant<int, 0>());
+    inverse(std::integral_constant<int, 1>());
+    inverse(std::integral_constant<int, 2>());
+    inverse(std::integral_constant<int, 3>());
+    inverse(std::integral_constant<int, 4>());
+    inverse(std::integral_constant<int, 5>());
+  }
 }
 
 // ------------------------------------------------------------------ x pass, adjoint
