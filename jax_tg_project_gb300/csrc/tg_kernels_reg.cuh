@@ -118,20 +118,26 @@ __global__ void __launch_bounds__(128, 3) kz_reg_kernel(const PassArgs<R> a) {
       return czero<C>();
     };
   };
-  // wait for field f's rows (5 - f later groups may still be in flight)
-  auto ready = [&](auto f_tag) {
-    constexpr int F_ = decltype(f_tag)::value;
-    cp_async_wait<5 - F_>();
-    __syncwarp();
-  };
-
   C u[3][E], m[3][E], z[E];
+  auto inverse = [&](int f) {  // staged field f -> z (after waiting for its rows)
+    switch (f) {  // 5 - f later commit groups may still be in flight
+      case 0: cp_async_wait<5>(); break;
+      case 1: cp_async_wait<4>(); break;
+      case 2: cp_async_wait<3>(); break;
+      case 3: cp_async_wait<2>(); break;
+      case 4: cp_async_wait<1>(); break;
+      default: cp_async_wait<0>(); break;
+    }
+    __syncwarp();
+    auto src = packed(stg + f * 2 * Hz);
+    auto dst = [&](int b, int r, int, C v) { z[b + r * NBL] = v; };
+    fft_column<Plan, +1, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
+  };
   auto inv_u = [&](auto c_tag) {
     constexpr int c = decltype(c_tag)::value;
-    ready(c_tag);
-    auto src = packed(stg + c * 2 * Hz);
-    auto dst = [&](int b, int r, int, C v) { u[c][b + r * NBL] = v; };
-    fft_column<Plan, +1, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
+    inverse(c);
+#pragma unroll
+    for (int q = 0; q < E; ++q) u[c][q] = z[q];
   };
   inv_u(std::integral_constant<int, 0>());
   inv_u(std::integral_constant<int, 1>());
@@ -140,13 +146,10 @@ __global__ void __launch_bounds__(128, 3) kz_reg_kernel(const PassArgs<R> a) {
   for (int c = 0; c < 3; ++c)
 #pragma unroll
     for (int q = 0; q < E; ++q) m[c][q] = czero<C>();
-  // m = u x omega, one vorticity component at a time (lines packed in .x / .y)
-  auto inv_w = [&](auto w_tag) {
+  // m = u x omega, one vorticity component at a time (lines packed in .x / .y); the three
+  // transforms share one FFT body, the accumulation is selected by a switch
+  auto accumulate = [&](auto w_tag) {
     constexpr int w = decltype(w_tag)::value;
-    ready(std::integral_constant<int, 3 + w>());
-    auto src = packed(stg + (3 + w) * 2 * Hz);
-    auto dst = [&](int b, int r, int, C v) { z[b + r * NBL] = v; };
-    fft_column<Plan, +1, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
     constexpr int c1 = (w + 1) % 3, c2 = (w + 2) % 3;
 #pragma unroll
     for (int q = 0; q < E; ++q) {
@@ -154,13 +157,36 @@ __global__ void __launch_bounds__(128, 3) kz_reg_kernel(const PassArgs<R> a) {
       m[c2][q] = mk<C>(m[c2][q].x - u[c1][q].x * z[q].x, m[c2][q].y - u[c1][q].y * z[q].y);
     }
   };
-  inv_w(std::integral_constant<int, 0>());
-  inv_w(std::integral_constant<int, 1>());
-  inv_w(std::integral_constant<int, 2>());
-  // forward transforms straight from the registers, Hermitian unpack by shuffle
-#pragma unroll
+#pragma unroll 1
+  for (int w = 0; w < 3; ++w) {
+    inverse(3 + w);
+    switch (w) {
+      case 0: accumulate(std::integral_constant<int, 0>()); break;
+      case 1: accumulate(std::integral_constant<int, 1>()); break;
+      default: accumulate(std::integral_constant<int, 2>()); break;
+    }
+  }
+  // forward transforms straight from the registers, Hermitian unpack by shuffle; the three
+  // share one FFT body (a loop over a uniform component, the input selected by a switch
+  // with compile-time register indices), which keeps the code small for the instruction cache
+#pragma unroll 1
   for (int c = 0; c < 3; ++c) {
-    auto src = [&](int, int q) -> C { return m[c][q]; };
+    C in[E];
+    switch (c) {
+      case 0:
+#pragma unroll
+        for (int q = 0; q < E; ++q) in[q] = m[0][q];
+        break;
+      case 1:
+#pragma unroll
+        for (int q = 0; q < E; ++q) in[q] = m[1][q];
+        break;
+      default:
+#pragma unroll
+        for (int q = 0; q < E; ++q) in[q] = m[2][q];
+        break;
+    }
+    auto src = [&](int, int q) -> C { return in[q]; };
     auto dst = [&](int b, int r, int, C v) { z[b + r * NBL] = v; };
     fft_column<Plan, -1, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
     // partner value Z(N-k) for k = t + P q: lane (P-t) mod P, slot E-1-q (t != 0) or
