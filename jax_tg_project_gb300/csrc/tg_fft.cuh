@@ -38,6 +38,35 @@ template <typename C> __device__ __forceinline__ C cmulc(C a, C b) {
   return mk<C>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
 }
 template <typename C> __device__ __forceinline__ C cscale(C a, decltype(C::x) s) { return mk<C>(a.x * s, a.y * s); }
+
+// FP32: the two lanes of a complex add, subtract or real scaling in one packed
+// instruction (add/sub/mul.rn.f32x2, sm_100 family); each lane rounds exactly like
+// the scalar instruction, so results are unchanged
+__device__ __forceinline__ unsigned long long pack2(float2 a) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+  return r;
+}
+__device__ __forceinline__ float2 unpack2(unsigned long long v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+template <> __device__ __forceinline__ float2 cadd<float2>(float2 a, float2 b) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
+  return unpack2(r);
+}
+template <> __device__ __forceinline__ float2 csub<float2>(float2 a, float2 b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
+  return unpack2(r);
+}
+template <> __device__ __forceinline__ float2 cscale<float2>(float2 a, float s) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(make_float2(s, s))));
+  return unpack2(r);
+}
 template <typename C> __device__ __forceinline__ C cconj(C a) { return mk<C>(a.x, -a.y); }
 // multiply by i*s (s = +1 or -1 at compile time, or any real)
 template <typename C> __device__ __forceinline__ C cmul_i(C a) { return mk<C>(-a.y, a.x); }
@@ -49,6 +78,18 @@ __device__ __forceinline__ C wconst(int m) {
   using Re = decltype(C::x);
   const int q = (m % R) * (96 / R);
   return mk<C>(Re(kCos96(q)), Re(DIR * kSin96(q)));
+}
+
+// a * W_R^m (m a constant after unrolling): quarter turns are exact rotations, the
+// others a complex multiply by the tabulated constant
+template <typename C, int R, int DIR>
+__device__ __forceinline__ C cmul_w(C a, int m) {
+  const int q = (m % R) * (96 / R);
+  if (q == 0) return a;
+  if (q == 48) return mk<C>(-a.x, -a.y);
+  if (q == 24) return (DIR > 0) ? mk<C>(-a.y, a.x) : mk<C>(a.y, -a.x);  // * i DIR
+  if (q == 72) return (DIR > 0) ? mk<C>(a.y, -a.x) : mk<C>(-a.y, a.x);  // * -i DIR
+  return cmul(a, wconst<C, R, DIR>(m));
 }
 
 // ------------------------------------------------------------------ codelets
@@ -100,7 +141,7 @@ __device__ __forceinline__ void dft(C* v) {
         if (n2 * k1 == 0) {
           t[n2 * A + k1] = a[k1];
         } else {
-          t[n2 * A + k1] = cmul(a[k1], wconst<C, R, DIR>(n2 * k1));
+          t[n2 * A + k1] = cmul_w<C, R, DIR>(a[k1], n2 * k1);
         }
       }
     }
