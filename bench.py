@@ -454,6 +454,13 @@ def run_ours(args, rank, world, local_rank):
                 "alg_bytes_per_launch": abytes[dom]}
     step_alg = step_bytes(n)
 
+    # GPU extras before the CPU baseline: the baseline's host thread pool is still busy
+    # for a while after it returns and would slow the host side of later GPU runs
+    extras = None
+    if rank == 0 and not args.no_extras:
+        extras = {"mhd_128": measure_mhd(), "ensemble_64": measure_ensemble(),
+                  "adjoint_128": measure_adjoint()}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         times = cpu_step_seconds(n, budget=args.cpu_budget)
@@ -461,11 +468,6 @@ def run_ours(args, rank, world, local_rank):
         cpu = {"value": len(times) / sum(times), "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{len(times)} RK4 step(s) of the {n}^3 TG workload by the reference JAX "
                          "algorithm restated in NumPy/SciPy FP64, FFTs threaded over all cores"}
-
-    extras = None
-    if rank == 0 and not args.no_extras:
-        extras = {"mhd_128": measure_mhd(), "ensemble_64": measure_ensemble(),
-                  "adjoint_128": measure_adjoint()}
 
     clocks = clk.summary()
     if rank == 0:

@@ -1694,42 +1694,92 @@ struct Adjoint {
       for (cudaEvent_t e : es) TG_CUDA(cudaStreamWaitEvent(st, e, 0), "stream wait");
       return TG_OK;
     };
-    for (int j = nsteps - 1; j >= 0; --j) {
-      if (j == nsteps - 1) {
-        if ((rc = fetch(j, Vb[j & 1], 0, v_free[j & 1], v_ready[j & 1]))) return rc;
+    // one backward step of V-buffer parity q (L and lam alternate with it too), enqueued on
+    // p->st; inside a capture the buffer-free events become external record nodes
+    const int J = nsteps - 1;
+    C* Lb[2] = {L, LA};
+    int kernels = 0;
+    auto step_work = [&](int q, bool capturing) -> int {
+      int r;
+      const int64_t before = p->launches;
+      const C* tp[4] = {Vb[q], N1, N2, N3};
+      const C* Lq = Lb[(J ^ q) & 1];
+      C* LAq = Lb[(J ^ q ^ 1) & 1];
+      auto record = [&](cudaEvent_t e) -> int {
+        TG_CUDA(cudaEventRecordWithFlags(e, p->st, capturing ? cudaEventRecordExternal : cudaEventRecordDefault),
+                "event record");
+        return TG_OK;
+      };
+      for (int s = 4; s >= 1; --s) {
+        if ((r = tape_x(OP_KX_ADJ_LOAD, s, tp, Lq, LAq, Gb, nullptr))) return r;
+        if (s == 3 && (r = record(n2_free))) return r;
+        if (s == 1 && (r = record(v_free[q]))) return r;
+        if ((r = tape_yz())) return r;
+        double* part = (s >= 2) ? dpart + (size_t)(4 - s) * pslots : nullptr;
+        if ((r = tape_x(OP_KX_ADJ_FWD, s, tp, Lq, LAq, s > 1 ? Gb : nullptr, part))) return r;
+        if (s == 4 && (r = record(n3_free))) return r;
+        if (s == 2 && (r = record(n1_free))) return r;
+      }
+      accumulate_partials_wide<<<1, 256, 0, p->st>>>(dpart, (int)(3 * pslots), dnu);
+      ++p->launches;
+      if ((r = launch_check("adjoint nu sum"))) return r;
+      kernels = (int)(p->launches - before);
+      return TG_OK;
+    };
+    // refill the buffers of step j - 1 once step j's readers are done (V: the other buffer)
+    auto fetch_next = [&](int j) -> int {
+      int r;
+      if ((r = fetch(j - 1, Vb[(j - 1) & 1], 0, v_free[(j - 1) & 1], v_ready[(j - 1) & 1]))) return r;
+      if ((r = fetch(j - 1, N3, 3, n3_free, n3_ready))) return r;
+      if ((r = fetch(j - 1, N2, 2, n2_free, n2_ready))) return r;
+      return fetch(j - 1, N1, 1, n1_free, n1_ready);
+    };
+    cudaGraphExec_t bx[2] = {nullptr, nullptr};
+    cudaGraph_t bg[2] = {nullptr, nullptr};
+    struct GraphGuard {  // the backward step graphs are released on every return path
+      cudaGraphExec_t* x;
+      cudaGraph_t* g;
+      ~GraphGuard() {
+        for (int k = 0; k < 2; ++k) {
+          if (x[k]) cudaGraphExecDestroy(x[k]);
+          if (g[k]) cudaGraphDestroy(g[k]);
+        }
+      }
+    } guard{bx, bg};
+    for (int j = J; j >= 0; --j) {
+      const int q = j & 1;
+      if (j == J) {
+        if ((rc = fetch(j, Vb[q], 0, v_free[q], v_ready[q]))) return rc;
         if ((rc = fetch(j, N3, 3, n3_free, n3_ready))) return rc;
         if ((rc = fetch(j, N2, 2, n2_free, n2_ready))) return rc;
         if ((rc = fetch(j, N1, 1, n1_free, n1_ready))) return rc;
       }
-      if ((rc = wait({v_ready[j & 1], n1_ready, n2_ready, n3_ready}))) return rc;
-      // V of the next step goes to the other V buffer, free since stage 1 of step j + 1
-      if (j > 0 && (rc = fetch(j - 1, Vb[(j - 1) & 1], 0, v_free[(j - 1) & 1], v_ready[(j - 1) & 1])))
-        return rc;
-      const C* tp[4] = {Vb[j & 1], N1, N2, N3};
-      for (int s = 4; s >= 1; --s) {
-        if ((rc = tape_x(OP_KX_ADJ_LOAD, s, tp, L, LA, Gb, nullptr))) return rc;
-        if (s == 3) {
-          TG_CUDA(cudaEventRecord(n2_free, st), "event record");
-          if (j > 0 && (rc = fetch(j - 1, N2, 2, n2_free, n2_ready))) return rc;
+      if ((rc = wait({v_ready[q], n1_ready, n2_ready, n3_ready}))) return rc;
+      if (j == J) {  // eagerly (sets the kernels' attributes outside capture), then one graph per parity
+        if ((rc = step_work(q, false))) return rc;
+        if (j > 0) {
+          if (!p->cap) TG_CUDA(cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking), "capture stream");
+          for (int k = 0; k < 2; ++k) {
+            cudaStream_t user = p->st;
+            TG_CUDA(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal), "begin capture");
+            const int64_t before = p->launches;
+            p->st = p->cap;
+            rc = step_work(k, true);
+            p->st = user;
+            p->launches = before;
+            cudaError_t e = cudaStreamEndCapture(p->cap, &bg[k]);
+            if (rc) return rc;
+            if (e != cudaSuccess) return cuda_fail(e, "adjoint end capture");
+            TG_CUDA(cudaGraphInstantiate(&bx[k], bg[k], 0), "adjoint graph instantiate");
+          }
         }
-        if (s == 1) TG_CUDA(cudaEventRecord(v_free[j & 1], st), "event record");
-        if ((rc = tape_yz())) return rc;
-        double* part = (s >= 2) ? dpart + (size_t)(4 - s) * pslots : nullptr;
-        if ((rc = tape_x(OP_KX_ADJ_FWD, s, tp, L, LA, s > 1 ? Gb : nullptr, part))) return rc;
-        if (s == 4) {
-          TG_CUDA(cudaEventRecord(n3_free, st), "event record");
-          if (j > 0 && (rc = fetch(j - 1, N3, 3, n3_free, n3_ready))) return rc;
-        }
-        if (s == 2) {
-          TG_CUDA(cudaEventRecord(n1_free, st), "event record");
-          if (j > 0 && (rc = fetch(j - 1, N1, 1, n1_free, n1_ready))) return rc;
-        }
+      } else {
+        TG_CUDA(cudaGraphLaunch(bx[q], st), "adjoint graph launch");
+        p->launches += kernels;
       }
-      accumulate_partials_wide<<<1, 256, 0, st>>>(dpart, (int)(3 * pslots), dnu);
-      ++p->launches;
-      if ((rc = launch_check("adjoint nu sum"))) return rc;
-      std::swap(L, LA);
+      if (j > 0 && (rc = fetch_next(j))) return rc;
     }
+    L = Lb[(J ^ 0 ^ 1) & 1];  // lam after step 0
     TG_CUDA(cudaMemcpyAsync(grad, L, fbytes, cudaMemcpyDeviceToDevice, st), "grad copy");
     TG_CUDA(cudaMemcpyAsync(grad_nu, dnu, sizeof(double), cudaMemcpyDeviceToDevice, st), "grad_nu copy");
     TG_CUDA(cudaStreamSynchronize(st), "adjoint sync");
