@@ -115,7 +115,7 @@ def measure_ensemble(steps=50, count=64):
     launches = ens.launches
     singles = []
     for r in runs:
-        p = tg.Plan(r.n)
+        p = tg.Plan(r.n, autotune=True)
         st = p.initial_condition("taylor_green", seed=1, pert_amp=1e-3, k0=4.0)
         p.step(st, dt=1e-3, nu=r.nu, nsteps=2)
         singles.append((p, st, r))
@@ -142,7 +142,8 @@ def measure_ensemble(steps=50, count=64):
         torch.cuda.synchronize()
         t1 = e0.elapsed_time(e1) / steps
         per_size[n] = {"runs": len(grp["idx"]), "batched_ms_per_step": tb, "single_run_ms_per_step": t1,
-                       "batching_gain": len(grp["idx"]) * t1 / tb}
+                       "batching_gain": len(grp["idx"]) * t1 / tb, "batched_variant": grp["plan"].variant,
+                       "single_variant": p.variant}
     pts = sum(r.n ** 3 for r in runs) * steps
     sizes = {n: sum(1 for r in runs if r.n == n) for n in sorted({r.n for r in runs})}
     return {"workload": f"ensemble_{count}_runs_fp32", "runs_per_size": sizes, "steps": steps,

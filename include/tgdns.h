@@ -52,9 +52,12 @@ enum { TG_PREC_F32 = 0, TG_PREC_F64 = 1 };
 enum {
   TG_FLAG_EXPLICIT_VISC = 1, /* classical RK4 with explicit viscosity (the reference's
                                 scheme) instead of the integrating-factor RK4 */
-  TG_FLAG_LORENTZ_REF = 2    /* momentum RHS uses -(j x b) as the reference CuPy MHD
+  TG_FLAG_LORENTZ_REF = 2,   /* momentum RHS uses -(j x b) as the reference CuPy MHD
                                 code does (cuda/taylor_green_mhd/operators.py:88-92)
                                 instead of the physical +(j x b) */
+  TG_FLAG_AUTOTUNE = 4       /* tg_plan_create times the pass variants (register-resident
+                                or shared-memory x and z passes) on this plan's shape and
+                                keeps the fastest (tg_pass_variant); no reference counterpart */
 };
 enum {
   TG_IC_TAYLOR_GREEN = 0,     /* u = (sin x cos y cos z, -cos x sin y cos z, 0); b = 0 */
@@ -184,6 +187,11 @@ int tg_physical_energy(tg_plan* plan, const void* phys, double* out);
 #define TG_PROF_SLOTS 12
 int tg_profile_passes(tg_plan* plan, void* state, double dt, double nu, double eta, int nsteps,
                       double ms[TG_PROF_SLOTS], int64_t count[TG_PROF_SLOTS]);
+
+/* Pass variant in use: bit 0 set = shared-memory z passes, bit 1 set = shared-memory x
+ * passes (0: register-resident passes where they are built).  Chosen by TG_FLAG_AUTOTUNE,
+ * else 0 (or the TG_PASS_VARIANT environment variable).  No reference counterpart. */
+int tg_pass_variant(const tg_plan* plan);
 
 /* Kernels launched by the last tg_step / tg_run call (for launch accounting). */
 int64_t tg_last_launch_count(const tg_plan* plan);

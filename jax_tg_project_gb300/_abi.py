@@ -17,7 +17,7 @@ c_int, c_int64, c_double, c_void_p, c_uint64 = (ctypes.c_int, ctypes.c_int64, ct
 TG_OK, TG_E_INVALID, TG_E_UNSUPPORTED, TG_E_CUDA, TG_E_NOMEM, TG_E_NONFINITE = range(6)
 TG_PHYS_HYDRO, TG_PHYS_MHD = 0, 1
 TG_PREC_F32, TG_PREC_F64 = 0, 1
-TG_FLAG_EXPLICIT_VISC, TG_FLAG_LORENTZ_REF = 1, 2
+TG_FLAG_EXPLICIT_VISC, TG_FLAG_LORENTZ_REF, TG_FLAG_AUTOTUNE = 1, 2, 4
 TG_IC_TAYLOR_GREEN, TG_IC_MHD_REFERENCE, TG_IC_MHD_EQUAL_ENERGY, TG_IC_ZERO = range(4)
 TG_ABSMAX_VELOCITY, TG_ABSMAX_DIVERGENCE = 0, 1
 TG_DERIVED_VORTICITY, TG_DERIVED_DIVERGENCE = 0, 1
@@ -67,6 +67,7 @@ SIGNATURES = {
     "tg_diagnostics_noalloc": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_double, c_double,
                                        c_void_p, c_void_p]),
     "tg_last_launch_count": (c_int64, [c_void_p]),
+    "tg_pass_variant": (c_int, [c_void_p]),
     "tg_last_error": (ctypes.c_char_p, []),
     "tg_version": (c_int, []),
 }

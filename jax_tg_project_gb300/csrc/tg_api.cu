@@ -661,7 +661,7 @@ struct tg_plan {
   const void* step_state = nullptr;
   int64_t launches = 0;
   int64_t scratch = 0;
-  int variant = 0;  // pass-kernel variant (TG_PASS_VARIANT=1 selects the shared-memory passes)
+  int variant = 0;  // pass variant: bit 0 shared-memory z passes, bit 1 shared-memory x passes
   // per-launch CUDA events (op, start, stop) while tg_profile_passes runs
   std::vector<ProfEvent>* prof = nullptr;
 };
@@ -974,6 +974,55 @@ extern "C" {
 const char* tg_last_error(void) { return g_last_error.c_str(); }
 int tg_version(void) { return 100; }
 
+// TG_FLAG_AUTOTUNE: time the distinct pass variants (register-resident or shared-memory
+// x and z passes) on this plan's shape -- graph-launched steps of a perturbed
+// Taylor-Green state -- and keep the fastest
+static int autotune(tg_plan* p) {
+  const bool f32 = p->prec == TG_PREC_F32;
+  const bool reg_z = f32 && has_reg_adjoint(p->n);                             // z: 16 ... 256
+  const bool reg_x = f32 && p->F == 3 && (has_reg_adjoint(p->n) || p->n == 96);  // x: hydro
+  std::vector<int> cands = {0};
+  if (reg_z) cands.push_back(1);
+  if (reg_x) cands.push_back(2);
+  if (reg_z && reg_x) cands.push_back(3);
+  if (cands.size() == 1) return TG_OK;
+  void* S = nullptr;
+  const size_t bytes = csize(p) * (size_t)p->batch * p->F * p->g.sS;
+  cudaError_t e = cudaMalloc(&S, bytes);
+  if (e != cudaSuccess) return cuda_fail(e, "autotune state");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = TG_OK, best = 0;
+  float best_ms = 1e30f;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) rc = TG_E_CUDA;
+  if (!rc) rc = tg_initial_condition(p, p->F == 6 ? TG_IC_MHD_EQUAL_ENERGY : TG_IC_TAYLOR_GREEN, 1, 1e-3, 4.0,
+                                     0.0, S);
+  for (int v : cands) {
+    if (rc) break;
+    p->variant = v;
+    drop_graph(p);
+    if ((rc = tg_step(p, S, 1e-4, 1e-2, 1e-2, 2))) break;  // eager step, capture, one replay
+    cudaEventRecord(e0, p->st);
+    if ((rc = tg_step(p, S, 1e-4, 1e-2, 1e-2, 3))) break;
+    cudaEventRecord(e1, p->st);
+    float ms = 0.0f;
+    if ((e = cudaEventSynchronize(e1)) != cudaSuccess || (e = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess) {
+      rc = cuda_fail(e, "autotune timing");
+      break;
+    }
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+  }
+  p->variant = best;
+  drop_graph(p);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(S);
+  p->launches = 0;
+  return rc;
+}
+
 int tg_plan_create(tg_plan** out, const tg_desc* d) {
   if (!out || !d) return fail(TG_E_INVALID, "tg_plan_create: null argument");
   *out = nullptr;
@@ -1069,9 +1118,18 @@ int tg_plan_create(tg_plan** out, const tg_desc* d) {
     tg_plan_destroy(p);
     return cuda_fail(e, "tg_plan_create: init");
   }
+  if ((p->flags & TG_FLAG_AUTOTUNE) && !std::getenv("TG_PASS_VARIANT")) {
+    const int rc = autotune(p);
+    if (rc) {
+      tg_plan_destroy(p);
+      return rc;
+    }
+  }
   *out = p;
   return TG_OK;
 }
+
+int tg_pass_variant(const tg_plan* p) { return p ? p->variant : 0; }
 
 int tg_plan_destroy(tg_plan* p) {
   if (!p) return TG_OK;

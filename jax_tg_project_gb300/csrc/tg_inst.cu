@@ -17,10 +17,14 @@
 
 namespace tg {
 cudaError_t TG_CAT(launch, TG_REAL, TG_N)(int op, const PassArgs<TG_REAL>& a, int runs, cudaStream_t st) {
+  // a.variant: bit 0 selects the shared-memory z passes, bit 1 the shared-memory x passes
+  const bool reg_z = (a.variant & 1) == 0, reg_x = (a.variant & 2) == 0;
+  (void)reg_z;
+  (void)reg_x;
   if constexpr (std::is_same<TG_REAL, float>::value && HasRegZ<TG_N>::value) {
-    if (a.variant == 0 && op == OP_KZ_PROD_HD) return launch_kz_reg<TG_REAL, TG_N>(a, runs, st);
-    if (a.variant == 0 && op == OP_KZ_PROD_MHD) return launch_kz_reg_mhd<TG_REAL, TG_N>(a, runs, st);
-    if (a.variant == 0 && op == OP_KZ_ADJ) return launch_kz_reg_adj<TG_REAL, TG_N>(a, runs, st);
+    if (reg_z && op == OP_KZ_PROD_HD) return launch_kz_reg<TG_REAL, TG_N>(a, runs, st);
+    if (reg_z && op == OP_KZ_PROD_MHD) return launch_kz_reg_mhd<TG_REAL, TG_N>(a, runs, st);
+    if (reg_z && op == OP_KZ_ADJ) return launch_kz_reg_adj<TG_REAL, TG_N>(a, runs, st);
     const bool tape = (a.flags & FLAG_TAPE) != 0;
     if (op == OP_KX_ADJ_LOAD)
       return tape ? launch_kx_reg_adj<TG_REAL, TG_N, KX_ADJ_LOAD_T>(a, runs, st)
@@ -31,7 +35,7 @@ cudaError_t TG_CAT(launch, TG_REAL, TG_N)(int op, const PassArgs<TG_REAL>& a, in
     if (op == OP_KX_NL_FWD) return launch_kx_reg_adj<TG_REAL, TG_N, KX_NL_FWD>(a, runs, st);
   }
   if constexpr (std::is_same<TG_REAL, float>::value && HasRegX<TG_N>::value) {
-    if (a.variant == 0) {
+    if (reg_x) {
       if (op == OP_KX_STAGE3) return launch_kx_reg<TG_REAL, TG_N, KX_STAGE>(a, runs, st);
       if (op == OP_KX_LOAD3 && a.map == MAP_UW && a.nin == 3 && a.nout == 6)
         return launch_kx_reg<TG_REAL, TG_N, KX_LOAD>(a, runs, st);

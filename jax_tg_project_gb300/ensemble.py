@@ -42,17 +42,18 @@ class Ensemble:
     """Independent runs advanced together.
 
     Run i of size group g gets the perturbation seed ``seed + 1000 * n_g + r``
-    where r is its index inside the group (the order of ``runs`` is kept).
+    where r is its index inside the group (the order of ``runs`` is kept).  With
+    ``autotune`` each group's plan picks its pass variant by timing on its own batch.
     """
 
     def __init__(self, runs, dt=1e-3, pert_amp=1e-3, k0=4.0, seed=0, precision="f32",
-                 concurrent=True):
+                 concurrent=True, autotune=True):
         self.runs = list(runs)
         self.dt = float(dt)
         self.groups = []
         for n in sorted({r.n for r in self.runs}):
             idx = [i for i, r in enumerate(self.runs) if r.n == n]
-            plan = Plan(n, batch=len(idx), precision=precision)
+            plan = Plan(n, batch=len(idx), precision=precision, autotune=autotune)
             plan.set_run_params(nu=[self.runs[i].nu for i in idx], eta=[0.0] * len(idx),
                                 dt=[self.dt] * len(idx))
             state = plan.initial_condition("taylor_green", seed=seed + 1000 * n, pert_amp=pert_amp,

@@ -31,7 +31,9 @@ class Plan:
     """A batch of ``batch`` independent runs on an ``n``^3 grid."""
 
     def __init__(self, n, batch=1, physics="hydro", precision="f32", explicit_viscosity=False,
-                 lorentz_sign=1.0, cutoff=0, device=None):
+                 lorentz_sign=1.0, cutoff=0, device=None, autotune=False):
+        """``autotune``: time the register-resident and shared-memory pass variants on this
+        shape when the plan is created and keep the fastest (``variant``)."""
         if not torch.cuda.is_available():
             raise RuntimeError("jax_tg_project_gb300 needs a CUDA device (no CPU path exists)")
         self.lib = _abi.load()
@@ -46,6 +48,8 @@ class Plan:
             flags |= _abi.TG_FLAG_EXPLICIT_VISC
         if lorentz_sign < 0:
             flags |= _abi.TG_FLAG_LORENTZ_REF
+        if autotune:
+            flags |= _abi.TG_FLAG_AUTOTUNE
         self.lorentz_sign = -1.0 if lorentz_sign < 0 else 1.0
         desc = _abi.TgDesc(self.n, self.batch, _PHYS[physics], _PREC[precision], flags, int(cutoff))
         h = ctypes.c_void_p()
@@ -88,6 +92,11 @@ class Plan:
         for d in self.state_shape:
             n *= d
         return n * (8 if self.precision == "f32" else 16)
+
+    @property
+    def variant(self):
+        """Pass variant in use: bit 0 = shared-memory z passes, bit 1 = shared-memory x passes."""
+        return int(self.lib.tg_pass_variant(self._h))
 
     @property
     def last_launch_count(self):

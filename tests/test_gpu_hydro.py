@@ -114,19 +114,38 @@ def test_batched_runs_are_independent():
 @pytest.mark.parametrize("N", [16, 32, 64, 128])
 def test_register_and_shared_memory_passes_agree(N, monkeypatch):
     """The register-resident x/z passes and the shared-memory passes are two
-    implementations of the same step; they agree to FP32 round-off."""
-    import torch
-    plans = []
-    for variant in ("0", "1"):
+    implementations of the same step; every mix of them (TG_PASS_VARIANT bit 0: z, bit 1:
+    x) agrees with the register-resident step to FP32 round-off."""
+    steps, rhss = [], []
+    for variant in ("0", "1", "2", "3"):
         monkeypatch.setenv("TG_PASS_VARIANT", variant)
         p = _plan(N, "f32")
+        assert p.variant == int(variant)
         s = p.initial_condition("taylor_green", seed=9, pert_amp=0.05, k0=3.0)
         p.step(s, dt=2e-3, nu=2e-3, nsteps=3)
-        plans.append(from_state(p, s)[0])
+        steps.append(from_state(p, s)[0])
         r = p.rhs(p.initial_condition("taylor_green", seed=9, pert_amp=0.05, k0=3.0), nu=2e-3)
-        plans.append(from_state(p, r)[0])
-    assert rel_l2(plans[0], plans[2]) < 2e-6
-    assert rel_l2(plans[1], plans[3]) < 2e-6
+        rhss.append(from_state(p, r)[0])
+    for k in range(1, 4):
+        assert rel_l2(steps[0], steps[k]) < 2e-6, k
+        assert rel_l2(rhss[0], rhss[k]) < 2e-6, k
+
+
+@pytest.mark.parametrize("N,physics", [(32, "hydro"), (96, "hydro"), (128, "hydro"), (64, "mhd")])
+def test_autotuned_plan_matches_default(N, physics, monkeypatch):
+    """TG_FLAG_AUTOTUNE picks one of the variants by timing; the step it runs agrees with
+    the default plan's to FP32 round-off."""
+    import jax_tg_project_gb300 as tg
+    monkeypatch.delenv("TG_PASS_VARIANT", raising=False)
+    ic = "mhd_equal_energy" if physics == "mhd" else "taylor_green"
+    outs = []
+    for auto in (False, True):
+        p = tg.Plan(N, physics=physics, precision="f32", autotune=auto)
+        assert p.variant in ((0, 1, 2, 3) if auto else (0,))
+        s = p.initial_condition(ic, seed=4, pert_amp=0.05, k0=3.0)
+        p.step(s, dt=1e-3, nu=2e-3, eta=2e-3, nsteps=3)
+        outs.append(from_state(p, s)[0])
+    assert rel_l2(outs[0], outs[1]) < 2e-6
 
 
 def test_fp32_step_tracks_fp64_gpu_run_at_256():
