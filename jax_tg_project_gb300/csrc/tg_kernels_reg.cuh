@@ -797,7 +797,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
 //                       + <L, -k^2 h E(h) V - k^2 h^2/6 (E(h) n1 + E(h/2) (n2 + n3))>
 //                s = 3: <g3, -k^2 h/2 E(h/2) V>;  s = 2: <g2, -k^2 h/2 a2>, a2 = E(h/2)(V + h/2 n1)
 template <typename R, int N, int MODE>
-__global__ void __launch_bounds__(KxRegShape<R, N>::NT, 2) kx_reg_adj_kernel(const PassArgs<R> a) {
+__global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) kx_reg_adj_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Sh = KxRegShape<R, N>;
   using Plan = typename Sh::Plan;
@@ -904,9 +904,20 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, 2) kx_reg_adj_kernel(con
         acc[c2][q] = mk<C>(acc[c2][q].x - R(kk[c1]) * iz.x, acc[c2][q].y - R(kk[c1]) * iz.y);
       }
     };
-    add_curl(std::integral_constant<int, 0>());
-    add_curl(std::integral_constant<int, 1>());
-    add_curl(std::integral_constant<int, 2>());
+    if constexpr (N >= 128) {  // one FFT body for the three q components (instruction cache)
+#pragma unroll 1
+      for (int c = 0; c < 3; ++c) {
+        switch (c) {
+          case 0: add_curl(std::integral_constant<int, 0>()); break;
+          case 1: add_curl(std::integral_constant<int, 1>()); break;
+          default: add_curl(std::integral_constant<int, 2>()); break;
+        }
+      }
+    } else {
+      add_curl(std::integral_constant<int, 0>());
+      add_curl(std::integral_constant<int, 1>());
+      add_curl(std::integral_constant<int, 2>());
+    }
     double dsum = 0.0;
 #pragma unroll
     for (int q = 0; q < E; ++q) {
@@ -984,15 +995,33 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, 2) kx_reg_adj_kernel(con
     C* xo = a.out + (long long)run * a.nout * g.sX + (long long)iyc * Hz + kz;
     const int gi0 = (a.nout == 3) ? 6 : 0;  // output field of GI = gi0 + slot
     C* xa = (TAPE && a.nout == 9) ? a.out2 + (long long)iyc * Hz + kz - 6 * g.sX : xo - gi0 * g.sX;
-    auto inverse_from = [&](auto gi_tag, auto* arr) {
-      constexpr int GI = decltype(gi_tag)::value;
-      auto src = [&](int k, int q) -> C {
-        const int ic = kcompact(k, N, K);
-        if (ic < 0) return czero<C>();
-        if constexpr (GI < 6) return uw_field<GI>(arr, q, float(ksigned(ic, K)), kyf, kzf);
-        else return arr[GI - 6][q];
+    // field gi of (u, omega, a) -> its inverse-x transform.  The values of this thread's
+    // modes are formed by a switch with compile-time register indices; at N >= 128 the
+    // fields loop over one FFT body (instruction cache), smaller transforms are unrolled.
+    auto field = [&](int gi, auto* arr) {
+      C in[E];
+      auto fill = [&](auto gi_tag) {
+        constexpr int GI = decltype(gi_tag)::value;
+#pragma unroll
+        for (int q = 0; q < E; ++q) {
+          const int ic = kcompact(t + P * q, N, K);
+          if constexpr (GI < 6) in[q] = (ic < 0) ? czero<C>() : uw_field<GI>(arr, q, float(ksigned(ic, K)), kyf, kzf);
+          else in[q] = (ic < 0) ? czero<C>() : arr[GI - 6][q];
+        }
       };
-      C* xg = (GI >= 6) ? xa + GI * g.sX : xo + (GI - gi0) * g.sX;
+      switch (gi) {
+        case 0: fill(std::integral_constant<int, 0>()); break;
+        case 1: fill(std::integral_constant<int, 1>()); break;
+        case 2: fill(std::integral_constant<int, 2>()); break;
+        case 3: fill(std::integral_constant<int, 3>()); break;
+        case 4: fill(std::integral_constant<int, 4>()); break;
+        case 5: fill(std::integral_constant<int, 5>()); break;
+        case 6: fill(std::integral_constant<int, 6>()); break;
+        case 7: fill(std::integral_constant<int, 7>()); break;
+        default: fill(std::integral_constant<int, 8>()); break;
+      }
+      C* xg = (gi >= 6) ? xa + gi * g.sX : xo + (gi - gi0) * g.sX;
+      auto src = [&](int, int q) -> C { return in[q]; };
       auto dst = [&](int, int, int xx, C val) {
         if (zok) xg[(long long)xx * M * Hz] = val;
       };
@@ -1030,9 +1059,13 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, 2) kx_reg_adj_kernel(con
       }
     }
     if (a.nout != 6) {
-      inverse_from(std::integral_constant<int, 6>(), acc);
-      inverse_from(std::integral_constant<int, 7>(), acc);
-      inverse_from(std::integral_constant<int, 8>(), acc);
+      if constexpr (N >= 128) {
+#pragma unroll 1
+        for (int gi = 6; gi < 9; ++gi) field(gi, acc);
+      } else {
+#pragma unroll
+        for (int gi = 6; gi < 9; ++gi) field(gi, acc);
+      }
     }
     if (a.nout != 3) {
       // the state whose u, curl u are transformed: spec_in, or the tape's stage state a_sl
@@ -1062,12 +1095,13 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, 2) kx_reg_adj_kernel(con
           v[f][q] = x;
         }
       }
-      inverse_from(std::integral_constant<int, 0>(), v);
-      inverse_from(std::integral_constant<int, 1>(), v);
-      inverse_from(std::integral_constant<int, 2>(), v);
-      inverse_from(std::integral_constant<int, 3>(), v);
-      inverse_from(std::integral_constant<int, 4>(), v);
-      inverse_from(std::integral_constant<int, 5>(), v);
+      if constexpr (N >= 128) {
+#pragma unroll 1
+        for (int gi = 0; gi < 6; ++gi) field(gi, v);
+      } else {
+#pragma unroll
+        for (int gi = 0; gi < 6; ++gi) field(gi, v);
+      }
     }
   }
 }
