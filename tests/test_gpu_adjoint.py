@@ -136,3 +136,17 @@ def test_host_tape_tracks_fp64_adjoint():
     assert float(l32) == pytest.approx(float(l64), rel=1e-6)
     assert rel_l2(from_state(p32, g32), from_state(p64, g64)) < 2e-5
     assert float(n32) == pytest.approx(float(n64), rel=1e-4)
+
+
+@pytest.mark.parametrize("N,cutoff,nsteps", [(32, 0, 1), (32, 7, 4), (64, 15, 3)])
+def test_host_tape_edge_cases(N, cutoff, nsteps):
+    """One step (the backward runs eagerly, no step graph) and cutoffs below N/3 (the
+    kernels' masks follow K): tape and checkpointed adjoints agree."""
+    import jax_tg_project_gb300 as tg
+    p = tg.Plan(N, precision="f32", cutoff=cutoff)
+    s0 = p.initial_condition("taylor_green", seed=11, pert_amp=0.05, k0=3.0)
+    lc, gc, nc = p.adjoint(s0, 2e-3, 1 / 300, nsteps, 1)
+    lt, gt, nt = p.adjoint(s0, 2e-3, 1 / 300, nsteps, "tape")
+    assert float(lt) == pytest.approx(float(lc), rel=1e-6)
+    assert rel_l2(from_state(p, gt), from_state(p, gc)) < 2e-5
+    assert float(nt) == pytest.approx(float(nc), rel=1e-4, abs=1e-9)

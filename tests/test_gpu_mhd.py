@@ -110,3 +110,18 @@ def test_mhd_register_and_shared_memory_passes_agree(N, monkeypatch):
         p.step(s, dt=1e-3, nu=2e-3, eta=3e-3, nsteps=3)
         outs.append(from_state(p, s)[0])
     assert rel_l2(outs[0], outs[1]) < 2e-6
+
+
+def test_autotuned_batched_mhd_plan_matches_runs_one_at_a_time():
+    """An autotuned batched MHD plan (per-run nu, eta) equals plain single-run plans."""
+    import jax_tg_project_gb300 as tg
+    nus, etas = [2e-3, 4e-3], [3e-3, 1e-3]
+    pb = tg.Plan(32, batch=2, physics="mhd", precision="f32", autotune=True)
+    sb = pb.initial_condition("mhd_equal_energy", seed=5, pert_amp=0.02, k0=3.0)
+    pb.set_run_params(nu=nus, eta=etas, dt=[1e-3, 1e-3])
+    pb.step(sb, nsteps=4)
+    for r in range(2):
+        p1 = tg.Plan(32, physics="mhd", precision="f32")
+        s1 = p1.initial_condition("mhd_equal_energy", seed=5 + r, pert_amp=0.02, k0=3.0)
+        p1.step(s1, dt=1e-3, nu=nus[r], eta=etas[r], nsteps=4)
+        assert rel_l2(from_state(p1, s1)[0], from_state(pb, sb)[r]) < 2e-6
