@@ -37,6 +37,19 @@ template <> struct RegPlan<128> { using T = FftPlan<128, 16, 8, 2, 8>; };
 template <> struct RegPlan<256> { using T = FftPlan<256, 32, 8, 4, 8>; };
 template <> struct RegPlan<96> { using T = FftPlan<96, 8, 4, 4, 6>; };  // E = 12: x pass only
 
+// Slot q of a thread holds the modes k = t + P q (0 <= t < P).  Every dealiasing cutoff
+// satisfies K <= N/3, so a slot lying wholly inside (N/3, N - N/3) only ever holds removed
+// modes, and a slot with P q > N/3 never holds a kept non-negative kz: both tests are
+// compile-time constants once the slot loops are unrolled.
+template <int N, int P> __host__ __device__ constexpr bool slot_cut(int q) {
+  return P * q > N / 3 && P * q + P - 1 < N - N / 3;
+}
+template <int N, int P> __host__ __device__ constexpr bool slot_past_k(int q) { return P * q > N / 3; }
+// compact index of the mode of slot q of thread t (-1: removed), constant for cut slots
+template <int N, int P> __device__ __forceinline__ int kcompact_slot(int t, int q, int K) {
+  return slot_cut<N, P>(q) ? -1 : kcompact(t + P * q, N, K);
+}
+
 // sizes with a register-resident z pass (E = 8; N = 8 has fewer line pairs than one
 // CTA holds) and with a register-resident x pass
 template <int N> struct HasRegZ { static constexpr bool value = (N == 16 || N == 32 || N == 64 || N == 128 || N == 256); };
@@ -105,7 +118,8 @@ __global__ void __launch_bounds__(128, 3) kz_reg_kernel(const PassArgs<R> a) {
 
   // Z = A + iB for rows (x, y0), (x, y0+1); kz > K is zero, kz < 0 by Hermitian symmetry
   auto packed = [&](const C* fld) {
-    return [=](int k, int) -> C {
+    return [=](int k, int q) -> C {
+      if (slot_cut<N, P>(q)) return czero<C>();
       if (k <= K) {
         C A = fld[k], B = fld[Hz + k];
         if (k == 0) { A.y = 0; B.y = 0; }
@@ -195,6 +209,7 @@ __global__ void __launch_bounds__(128, 3) kz_reg_kernel(const PassArgs<R> a) {
     const int src_lane = (P - t) % P;
 #pragma unroll
     for (int qq = 0; qq < E; ++qq) {
+      if (slot_past_k<N, P>(E - 1 - qq)) continue;  // zm of a slot that is never stored
       C v;
       v.x = __shfl_sync(0xffffffffu, z[qq].x, src_lane, P);
       v.y = __shfl_sync(0xffffffffu, z[qq].y, src_lane, P);
@@ -203,6 +218,7 @@ __global__ void __launch_bounds__(128, 3) kz_reg_kernel(const PassArgs<R> a) {
     C* outf = zout + c * g.sY + row0;
 #pragma unroll
     for (int q = 0; q < E; ++q) {
+      if (slot_past_k<N, P>(q)) continue;
       const int k = t + P * q;
       if (k <= K) {
         outf[k] = mk<C>((z[q].x + zm[q].x) * R(0.5), (z[q].y - zm[q].y) * R(0.5));
@@ -270,7 +286,8 @@ __global__ void __launch_bounds__(128) kz_reg_mhd_kernel(const PassArgs<R> a) {
   const R sl = R(a.coef[run].lorentz);
 
   auto packed = [&](const C* fld) {
-    return [=](int k, int) -> C {
+    return [=](int k, int q) -> C {
+      if (slot_cut<N, P>(q)) return czero<C>();
       if (k <= K) {
         C A = fld[k], B = fld[Hz + k];
         if (k == 0) { A.y = 0; B.y = 0; }
@@ -284,7 +301,8 @@ __global__ void __launch_bounds__(128) kz_reg_mhd_kernel(const PassArgs<R> a) {
     };
   };
   auto packed_g = [&](const C* fld) {  // j: straight from global memory
-    return [=](int k, int) -> C {
+    return [=](int k, int q) -> C {
+      if (slot_cut<N, P>(q)) return czero<C>();
       if (k <= K) {
         C A = fld[row0 + k], B = fld[row0 + Hz + k];
         if (k == 0) { A.y = 0; B.y = 0; }
@@ -306,6 +324,7 @@ __global__ void __launch_bounds__(128) kz_reg_mhd_kernel(const PassArgs<R> a) {
     const int src_lane = (P - t) % P;
 #pragma unroll
     for (int qq = 0; qq < E; ++qq) {
+      if (slot_past_k<N, P>(E - 1 - qq)) continue;  // zm of a slot that is never stored
       C v;
       v.x = __shfl_sync(0xffffffffu, z[qq].x, src_lane, P);
       v.y = __shfl_sync(0xffffffffu, z[qq].y, src_lane, P);
@@ -314,6 +333,7 @@ __global__ void __launch_bounds__(128) kz_reg_mhd_kernel(const PassArgs<R> a) {
     C* outf = zout + c * g.sY + row0;
 #pragma unroll
     for (int q = 0; q < E; ++q) {
+      if (slot_past_k<N, P>(q)) continue;
       const int k = t + P * q;
       if (k <= K) {
         outf[k] = mk<C>((z[q].x + zm[q].x) * R(0.5), (z[q].y - zm[q].y) * R(0.5));
@@ -455,7 +475,8 @@ __global__ void __launch_bounds__(128, 3) kz_reg_adj_kernel(const PassArgs<R> a)
   __syncthreads();
   const WarpSync ws;
   auto packed = [&](const C* fld) {
-    return [=](int k, int) -> C {
+    return [=](int k, int q) -> C {
+      if (slot_cut<N, P>(q)) return czero<C>();
       if (k <= K) {
         C A = fld[k], B = fld[Hz + k];
         if (k == 0) { A.y = 0; B.y = 0; }
@@ -476,6 +497,7 @@ __global__ void __launch_bounds__(128, 3) kz_reg_adj_kernel(const PassArgs<R> a)
     const int src_lane = (P - t) % P;
 #pragma unroll
     for (int qq = 0; qq < E; ++qq) {
+      if (slot_past_k<N, P>(E - 1 - qq)) continue;  // zm of a slot that is never stored
       C v;
       v.x = __shfl_sync(0xffffffffu, z[qq].x, src_lane, P);
       v.y = __shfl_sync(0xffffffffu, z[qq].y, src_lane, P);
@@ -484,6 +506,7 @@ __global__ void __launch_bounds__(128, 3) kz_reg_adj_kernel(const PassArgs<R> a)
     C* outf = zout + c * g.sY + row0;
 #pragma unroll
     for (int q = 0; q < E; ++q) {
+      if (slot_past_k<N, P>(q)) continue;
       const int k = t + P * q;
       if (k <= K) {
         outf[k] = mk<C>((z[q].x + zm[q].x) * R(0.5), (z[q].y - zm[q].y) * R(0.5));
@@ -665,7 +688,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
     for (int f = 0; f < 3; ++f)
 #pragma unroll
       for (int q = 0; q < E; ++q) {
-        const int ic = kcompact(t + P * q, N, K);
+        const int ic = kcompact_slot<N, P>(t, q, K);
         v[f][q] = (zok && ic >= 0) ? sin_[((long long)f * M + ic) * M * Hz] : czero<C>();
       }
   } else {
@@ -699,7 +722,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
     const R h = R(cf.dt);
 #pragma unroll
     for (int q = 0; q < E; ++q) {
-      const int ic = kcompact(t + P * q, N, K);
+      const int ic = kcompact_slot<N, P>(t, q, K);
       if (zok && ic >= 0) {
         const float kx = float(ksigned(ic, K));
         const float k2 = kx * kx + kyf * kyf + kzf * kzf;
@@ -741,7 +764,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
     constexpr int GI = decltype(gi_tag)::value;
 #pragma unroll
     for (int q = 0; q < E; ++q) {
-      const int ic = kcompact(t + P * q, N, K);
+      const int ic = kcompact_slot<N, P>(t, q, K);
       in[q] = (ic < 0) ? czero<C>() : uw_field<GI>(v, q, float(ksigned(ic, K)), kyf, kzf);
     }
   };
@@ -864,7 +887,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
     }
 #pragma unroll
     for (int q = 0; q < E; ++q) {
-      const int ic = kcompact(t + P * q, N, K);
+      const int ic = kcompact_slot<N, P>(t, q, K);
       if (zok && ic >= 0) {
         const float kx = float(ksigned(ic, K));
         leray(nv[0][q], nv[1][q], nv[2][q], kx, kyf, kzf, kx * kx + kyf * kyf + kzf * kzf);
@@ -894,7 +917,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
       fwd_to(3 + c, z);
 #pragma unroll
       for (int q = 0; q < E; ++q) {
-        const int ic = kcompact(t + P * q, N, K);
+        const int ic = kcompact_slot<N, P>(t, q, K);
         const float kx = float(ksigned(ic < 0 ? 0 : ic, K));
         const float kk[3] = {kx, kyf, kzf};
         // (k x e_c q)_{c+1} = k_{c+2} q,  (k x e_c q)_{c+2} = -k_{c+1} q; then times i
@@ -921,7 +944,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
     double dsum = 0.0;
 #pragma unroll
     for (int q = 0; q < E; ++q) {
-      const int ic = kcompact(t + P * q, N, K);
+      const int ic = kcompact_slot<N, P>(t, q, K);
       if (zok && ic >= 0) {
         if constexpr (!TAPE) {
 #pragma unroll
@@ -1004,7 +1027,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
         constexpr int GI = decltype(gi_tag)::value;
 #pragma unroll
         for (int q = 0; q < E; ++q) {
-          const int ic = kcompact(t + P * q, N, K);
+          const int ic = kcompact_slot<N, P>(t, q, K);
           if constexpr (GI < 6) in[q] = (ic < 0) ? czero<C>() : uw_field<GI>(arr, q, float(ksigned(ic, K)), kyf, kzf);
           else in[q] = (ic < 0) ? czero<C>() : arr[GI - 6][q];
         }
@@ -1030,7 +1053,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
     {  // mu (projected) into acc: plain S, or the tape seeds
 #pragma unroll
       for (int q = 0; q < E; ++q) {
-        const int ic = kcompact(t + P * q, N, K);
+        const int ic = kcompact_slot<N, P>(t, q, K);
         const bool ok = zok && ic >= 0;
         R cl = R(1), cg = R(0);
         if (TAPE && ok) {
@@ -1072,7 +1095,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
       C v[3][E];
 #pragma unroll
       for (int q = 0; q < E; ++q) {
-        const int ic = kcompact(t + P * q, N, K);
+        const int ic = kcompact_slot<N, P>(t, q, K);
         const bool ok = zok && ic >= 0;
         R kk = R(0), m1 = R(0), mh = R(0);
         if (TAPE && ok && sl > 1) factors(ic, kk, m1, mh);

@@ -10,7 +10,8 @@ from oracle import tg_numpy as T
 pytestmark = pytest.mark.gpu
 
 
-def test_ensemble_runs_equal_single_runs():
+def test_ensemble_runs_equal_single_runs(monkeypatch):
+    """Bit-identical: each single run uses the pass variant its autotuned group chose."""
     import torch
 
     import jax_tg_project_gb300 as tg
@@ -23,6 +24,7 @@ def test_ensemble_runs_equal_single_runs():
     for i, r in enumerate(runs):
         plan_b, sb = ens.state_of(i)
         grp = next(g for g in ens.groups if g["n"] == r.n)
+        monkeypatch.setenv("TG_PASS_VARIANT", str(grp["plan"].variant))
         p1 = tg.Plan(r.n)
         s1 = p1.initial_condition("taylor_green", seed=5 + 1000 * r.n + grp["idx"].index(i),
                                   pert_amp=1e-2, k0=3.0)
