@@ -116,4 +116,18 @@ __device__ __forceinline__ int kcompact(int k, int N, int K) {
 // full-axis frequency row of compact index i
 __device__ __forceinline__ int kfull(int i, int N, int K) { return i <= K ? i : i + N - (2 * K + 1); }
 
+// Slot q of a thread holds the modes k = t + P q (0 <= t < P).  Every dealiasing cutoff
+// satisfies K <= N/3, so a slot lying wholly inside (N/3, N - N/3) only ever holds removed
+// modes, and a slot with P q > N/3 never holds a kept non-negative kz: both tests are
+// compile-time constants once the slot loops are unrolled.
+template <int N, int P> __host__ __device__ constexpr bool slot_cut(int q) {
+  return P * q > N / 3 && P * q + P - 1 < N - N / 3;
+}
+template <int N, int P> __host__ __device__ constexpr bool slot_past_k(int q) { return P * q > N / 3; }
+// compact index of the mode of slot q of thread t (-1: removed), constant for cut slots
+template <int N, int P> __device__ __forceinline__ int kcompact_slot(int t, int q, int K) {
+  return slot_cut<N, P>(q) ? -1 : kcompact(t + P * q, N, K);
+}
+
+
 }  // namespace tg

@@ -164,7 +164,8 @@ kx_kernel(const PassArgs<R> a) {
     for (int f = 0; f < a.nin; ++f) {
       const C* wf = win + f * g.sX;
       auto src = [&](int x, int) -> C { return zok ? wf[(long long)x * M * Hz] : czero<C>(); };
-      auto dst = [&](int, int, int k, C v) {
+      auto dst = [&](int b, int r, int k, C v) {
+        if (slot_cut<N, P>(out_slot<Plan>(b, r))) return;  // always-removed modes
         const int ic = kcompact(k, N, K);
         if (ic >= 0) sb[(f * M + ic) * TZ + col] = cscale(v, inv_n3);
       };
@@ -253,7 +254,8 @@ kx_kernel(const PassArgs<R> a) {
     const int map = (MODE == KX_STAGE) ? (F == 6 ? MAP_UWBJ : MAP_UW) : a.map;
     C* xo = a.out + (long long)run * a.nout * g.sX + (long long)iyc * Hz + kz;
     for (int gi = 0; gi < a.nout; ++gi) {
-      auto src = [&](int k, int) -> C {
+      auto src = [&](int k, int q) -> C {
+        if (slot_cut<N, P>(q)) return czero<C>();  // always-removed modes
         const int ic = kcompact(k, N, K);
         if (!zok || ic < 0) return czero<C>();
         return field_value<C>(map, gi, sb, ic, col, M, TZ, float(ksigned(ic, K)), kyf, kzf);
@@ -290,7 +292,8 @@ ky_kernel(const PassArgs<R> a) {
   if constexpr (DIR > 0) {
     const C* in = a.in + ((long long)run * a.nin + f) * g.sX + (long long)x * M * Hz + kz;
     C* out = a.out + ((long long)run * a.nin + f) * g.sY + (long long)x * N * Hz + kz;
-    auto src = [&](int k, int) -> C {
+    auto src = [&](int k, int q) -> C {
+      if (slot_cut<N, P>(q)) return czero<C>();  // always-removed rows
       const int ic = kcompact(k, N, K);
       return (zok && ic >= 0) ? in[(long long)ic * Hz] : czero<C>();
     };
@@ -302,7 +305,8 @@ ky_kernel(const PassArgs<R> a) {
     const C* in = a.in + ((long long)run * a.nin + f) * g.sY + (long long)x * N * Hz + kz;
     C* out = a.out + ((long long)run * a.nin + f) * g.sX + (long long)x * M * Hz + kz;
     auto src = [&](int y, int) -> C { return zok ? in[(long long)y * Hz] : czero<C>(); };
-    auto dst = [&](int, int, int k, C v) {
+    auto dst = [&](int b, int r, int k, C v) {
+      if (slot_cut<N, P>(out_slot<Plan>(b, r))) return;  // always-removed rows
       const int ic = kcompact(k, N, K);
       if (zok && ic >= 0) out[(long long)ic * Hz] = v;
     };
@@ -348,7 +352,8 @@ kz_kernel(const PassArgs<R> a) {
 
   // Hermitian packing of rows (x,y0) and (x,y0+1) of one spectral field: Z = A + iB
   auto packed = [&](const C* fld) {
-    return [=](int k, int) -> C {
+    return [=](int k, int q) -> C {
+      if (slot_cut<N, Plan::P>(q)) return czero<C>();  // always-removed modes
       if (k <= K) {
         C A = fld[row0 + k], B = fld[row0 + Hz + k];
         if (k == 0) { A.y = 0; B.y = 0; }

@@ -37,19 +37,6 @@ template <> struct RegPlan<128> { using T = FftPlan<128, 16, 8, 2, 8>; };
 template <> struct RegPlan<256> { using T = FftPlan<256, 32, 8, 4, 8>; };
 template <> struct RegPlan<96> { using T = FftPlan<96, 8, 4, 4, 6>; };  // E = 12: x pass only
 
-// Slot q of a thread holds the modes k = t + P q (0 <= t < P).  Every dealiasing cutoff
-// satisfies K <= N/3, so a slot lying wholly inside (N/3, N - N/3) only ever holds removed
-// modes, and a slot with P q > N/3 never holds a kept non-negative kz: both tests are
-// compile-time constants once the slot loops are unrolled.
-template <int N, int P> __host__ __device__ constexpr bool slot_cut(int q) {
-  return P * q > N / 3 && P * q + P - 1 < N - N / 3;
-}
-template <int N, int P> __host__ __device__ constexpr bool slot_past_k(int q) { return P * q > N / 3; }
-// compact index of the mode of slot q of thread t (-1: removed), constant for cut slots
-template <int N, int P> __device__ __forceinline__ int kcompact_slot(int t, int q, int K) {
-  return slot_cut<N, P>(q) ? -1 : kcompact(t + P * q, N, K);
-}
-
 // sizes with a register-resident z pass (E = 8; N = 8 has fewer line pairs than one
 // CTA holds) and with a register-resident x pass
 template <int N> struct HasRegZ { static constexpr bool value = (N == 16 || N == 32 || N == 64 || N == 128 || N == 256); };
