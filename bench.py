@@ -235,6 +235,13 @@ def measure_adjoint(n=128, nsteps=256):
     return out
 
 
+def workload_config(n, world):
+    """The workload both arms report (the reference arm computes it in FP64 on the CPU)."""
+    return {"workload": f"taylor_green_hydro_{n}^3_fp32", "n": n, "nu": NU, "dt": DT,
+            "ic": "Taylor-Green", "l2": "inputs larger than L2 (no flush)",
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
 def step_bytes(n, F=3, csize=8):
     b = algorithmic_bytes(n, F=F, csize=csize)
     return 4 * sum(b.values())
@@ -356,8 +363,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
         "steps": len(times), "warmup": len(warm), "ms_per_step": 1e3 * sum(times) / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": f"taylor_green_hydro_{n}^3", "n": n, "nu": NU,
-                                         "dt": DT},
+        "data": "synthetic", "config": workload_config(n, world),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{len(times)} RK4 step(s) at {n}^3 of the reference JAX "
                                    "algorithm restated in NumPy/SciPy FP64 (jax is not installed); "
@@ -476,9 +482,7 @@ def run_ours(args, rank, world, local_rank):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"taylor_green_hydro_{n}^3_fp32", "n": n, "nu": NU, "dt": DT,
-                       "ic": "Taylor-Green", "l2": "inputs larger than L2 (no flush)",
-                       "parallelism": "replicas" if world > 1 else "single"},
+            "config": workload_config(n, world),
             "grid_point_updates_per_s": value * n ** 3,
             "hbm_step_bytes_model": step_alg,
             "step_gbs": step_alg / (ms_max / K * 1e-3) / 1e9,
