@@ -235,6 +235,17 @@ def measure_adjoint(n=128, nsteps=256):
     return out
 
 
+def replica_throughput(local_ms, steps, world, device="cpu"):
+    """Replicas (one process per GPU, no collective on the data path): the job time is the
+    slowest rank's, and the job processed world * steps steps.  Returns (ms_max, steps/s)."""
+    import torch
+    t = torch.tensor([float(local_ms)], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    return ms_max, world * steps / (ms_max / 1e3)
+
+
 def workload_config(n, world):
     """The workload both arms report (the reference arm computes it in FP64 on the CPU)."""
     return {"workload": f"taylor_green_hydro_{n}^3_fp32", "n": n, "nu": NU, "dt": DT,
@@ -405,12 +416,7 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.synchronize(dev)
         barrier()
     launches = plan.last_launch_count
-    ms = e0.elapsed_time(e1)
-    t = torch.tensor([ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = world * K / (ms_max / 1e3)
+    ms_max, value = replica_throughput(e0.elapsed_time(e1), K, world, dev)
 
     # ---- end to end through the public API with host buffers
     e2e = None
@@ -431,11 +437,9 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.synchronize(dev)
         barrier()
         e2e_launches = plan.last_launch_count
-        t2 = torch.tensor([e2.elapsed_time(e3)], dtype=torch.float64, device=dev)
-        if world > 1:
-            torch.distributed.all_reduce(t2, op=torch.distributed.ReduceOp.MAX)
+        _, e2e_value = replica_throughput(e2.elapsed_time(e3), K, world, dev)
         sbytes = init_host.numel() * init_host.element_size()
-        e2e = {"value": world * K / (float(t2.item()) / 1e3), "unit": UNIT,
+        e2e = {"value": e2e_value, "unit": UNIT,
                "h2d_bytes_per_step": sbytes / K,
                "d2h_bytes_per_step": (sbytes + series_host.numel() * 8) / K,
                "path": "Plan.run (tg_run via ctypes): initial state H2D from pinned host memory, "

@@ -38,6 +38,19 @@ def draw_runs(count=64, seed=2024, sizes=(32, 64, 96), re_range=(100.0, 3200.0))
     return [RunSpec(int(n), float(r)) for n, r in zip(ns, res)]
 
 
+def shard_runs(runs, rank, world):
+    """Indices of ``runs`` that rank ``rank`` of ``world`` advances: the runs are independent,
+    so an ensemble spread over GPUs needs no collective.  Longest-processing-time order
+    (cost n^3, ties by index) onto the least loaded rank, the same on every rank."""
+    load = [0] * world
+    owner = [0] * len(runs)
+    for i in sorted(range(len(runs)), key=lambda i: (-runs[i].n ** 3, i)):
+        r = min(range(world), key=lambda k: (load[k], k))
+        owner[i] = r
+        load[r] += runs[i].n ** 3
+    return [i for i in range(len(runs)) if owner[i] == rank]
+
+
 class Ensemble:
     """Independent runs advanced together.
 
