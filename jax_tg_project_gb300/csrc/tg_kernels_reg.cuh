@@ -947,8 +947,8 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
             const C gs = acc[f][q];
             if (a.spec_out != nullptr) a.spec_out[o] = gs;
             C lam;
-            C l = czero<C>();
-            if (st >= 2) l = a.S[o];
+            C l = czero<C>();  // L is read at stage 4 only (lam seed and its nu term)
+            if (st == 4) l = a.S[o];
             if (st == 4) {
               lam = mk<C>(e1 * (l.x + gs.x), e1 * (l.y + gs.y));
             } else {
