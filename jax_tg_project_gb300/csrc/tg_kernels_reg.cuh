@@ -239,7 +239,7 @@ struct KzRegMhdShape {
 };
 
 template <typename R, int N>
-__global__ void __launch_bounds__(128) kz_reg_mhd_kernel(const PassArgs<R> a) {
+__global__ void __launch_bounds__(128, 3) kz_reg_mhd_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Sh = KzRegMhdShape<R, N>;
   using Plan = typename Sh::Plan;
