@@ -211,6 +211,10 @@ int64_t tg_last_launch_count(const tg_plan* plan);
  * jax/taylor_green_jax.py:188-196.  Allocates its device work buffers for the call and
  * synchronises the stream. */
 #define TG_ADJ_HOST_TAPE (-1)
+
+/* Free the pinned host memory a TG_ADJ_HOST_TAPE adjoint keeps in the plan for later calls
+ * (the plan stays usable; the next tape adjoint pins it again).  No reference counterpart. */
+int tg_release_host_tape(tg_plan* plan);
 int tg_adjoint(tg_plan* plan, const void* state0, double dt, double nu, int nsteps, int checkpoint_every,
                void* grad_state, double* grad_nu, double* loss);
 

@@ -1131,6 +1131,17 @@ int tg_plan_create(tg_plan** out, const tg_desc* d) {
 
 int tg_pass_variant(const tg_plan* p) { return p ? p->variant : 0; }
 
+int tg_release_host_tape(tg_plan* p) {
+  if (!p) return fail(TG_E_INVALID, "tg_release_host_tape: null plan");
+  if (p->htape) {
+    const cudaError_t e = cudaFreeHost(p->htape);
+    p->htape = nullptr;
+    p->htape_bytes = 0;
+    if (e != cudaSuccess) return cuda_fail(e, "tg_release_host_tape");
+  }
+  return TG_OK;
+}
+
 int tg_plan_destroy(tg_plan* p) {
   if (!p) return TG_OK;
   drop_graph(p);

@@ -261,6 +261,10 @@ class Plan:
                                   ctypes.c_void_p(out.data_ptr() + 8)))
         return out[1], grad, out[0]
 
+    def release_tape(self):
+        """Free the pinned host memory a ``checkpoint_every="tape"`` adjoint keeps for later calls."""
+        check(self.lib.tg_release_host_tape(self._h))
+
     def energy_spectrum(self, state):
         """E(k) per run: (batch, bins) hydro or (batch, 2, bins) MHD (kinetic, magnetic)."""
         self._check_state(state)

@@ -121,10 +121,13 @@ def test_host_tape_adjoint_matches_checkpointed(N, nsteps):
     assert float(lt) == pytest.approx(float(lc), rel=1e-6)
     assert rel_l2(from_state(p, gt), from_state(p, gc)) < 2e-5
     assert float(nt) == pytest.approx(float(nc), rel=1e-4)
-    # a second call reuses the plan's host tape
+    # a second call reuses the plan's host tape; after a release the next call pins it again
     lt2, gt2, nt2 = p.adjoint(s0, dt, nu, nsteps, "tape")
     assert float(lt2) == float(lt) and float(nt2) == float(nt)
     assert bool((gt2 == gt).all())
+    p.release_tape()
+    lt3, gt3, nt3 = p.adjoint(s0, dt, nu, nsteps, "tape")
+    assert float(nt3) == float(nt) and bool((gt3 == gt).all())
 
 
 def test_host_tape_tracks_fp64_adjoint():
