@@ -271,10 +271,10 @@ kx_kernel(const PassArgs<R> a) {
 
 // ------------------------------------------------------------------ y pass
 template <typename R, int N, int DIR>
-__global__ void __launch_bounds__(PlanFor<N>::T::P * TileZ<R, N, 3>::base)
+__global__ void __launch_bounds__(YPlanFor<N>::T::P * TileZ<R, N, 3>::base)
 ky_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
-  using Plan = typename PlanFor<N>::T;
+  using Plan = typename YPlanFor<N>::T;
   constexpr int P = Plan::P, TZ = TileZ<R, N, 3>::base, CS = ColLayout<N>::CS, NT = P * TZ;
   const Geo g = a.g;
   const int K = g.K, M = g.M, Hz = g.Hz;
@@ -617,7 +617,7 @@ static cudaError_t launch_kx(const PassArgs<R>& a, int runs, cudaStream_t st) {
 template <typename R, int N, int DIR>
 static cudaError_t launch_ky(const PassArgs<R>& a, int runs, cudaStream_t st) {
   constexpr int TZ = TileZ<R, N, 3>::base;
-  constexpr int NT = PlanFor<N>::T::P * TZ;
+  constexpr int NT = YPlanFor<N>::T::P * TZ;
   const long long smem = (long long)sizeof(cplx<R>) * (N + TZ * ColLayout<N>::CS);
   static cudaError_t attr = set_smem(ky_kernel<R, N, DIR>, smem);
   if (attr != cudaSuccess) return attr;

@@ -181,3 +181,33 @@ def test_run_reports_non_finite_state():
     good = p.initial_condition("taylor_green")
     series = p.run(good, dt=0.005, nu=0.01, nsteps=4, save_every=2)
     assert torch.isfinite(series).all()
+
+
+def test_512_transforms_and_early_steps_match_256():
+    """512^3 (shared-memory passes): the forward / inverse transforms round-trip, and a few
+    early steps of Taylor-Green agree with the 256^3 run on the modes both keep (the flow is
+    still band-limited far below both cutoffs, so only round-off separates them)."""
+    import torch
+
+    import jax_tg_project_gb300 as tg
+    p5 = tg.Plan(512, precision="f32")
+    s5 = p5.initial_condition("taylor_green")
+    u = p5.inverse(s5)
+    back = p5.forward(u)
+    assert rel_l2(from_state(p5, back)[0], from_state(p5, s5)[0]) < 1e-6
+    p2 = tg.Plan(256, precision="f32")
+    s2 = p2.initial_condition("taylor_green")
+    for p, s in ((p5, s5), (p2, s2)):
+        p.step(s, dt=2e-3, nu=1 / 1600, nsteps=3)
+    d5 = p5.diagnostics(s5, nu=1 / 1600).cpu().numpy()[0]
+    d2 = p2.diagnostics(s2, nu=1 / 1600).cpu().numpy()[0]
+    np.testing.assert_allclose(d5[:3], d2[:3], rtol=1e-6)
+    # the coefficients |k| <= 4 (compact index ranges of both grids)
+    c5, c2 = from_state(p5, s5)[0], from_state(p2, s2)[0]
+    k5 = [i for i in range(c5.shape[1]) if min(i, c5.shape[1] - i) <= 4]
+    k2 = [i for i in range(c2.shape[1]) if min(i, c2.shape[1] - i) <= 4]
+    lo5 = c5[:, k5][:, :, k5][..., :5]
+    lo2 = c2[:, k2][:, :, k2][..., :5]
+    assert rel_l2(lo5, lo2) < 1e-5
+    del p5, p2
+    torch.cuda.empty_cache()
