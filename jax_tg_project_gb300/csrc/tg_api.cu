@@ -1691,9 +1691,10 @@ struct Adjoint {
     if ((rc = alloc((void**)&slot, 8 * fbytes))) return rc;
     if ((rc = alloc((void**)&cur0, fbytes))) return rc;
     if ((rc = alloc((void**)&dnu, sizeof(double)))) return rc;
-    // partial sums: stages 4, 3, 2, one slot per CTA of the x pass (at most M x Hk CTAs);
-    // slots a smaller grid leaves unwritten stay zero
-    const size_t pslots = (size_t)g.M * g.Hk;
+    // partial sums: stages 4, 3, 2, one slot per CTA of the x pass (its CTAs hold groups of
+    // four consecutive kz, so there are at most M x ceil(Hk / 4)); slots a grid with several
+    // groups per CTA leaves unwritten stay zero
+    const size_t pslots = (size_t)g.M * ((g.Hk + 3) / 4);
     if ((rc = alloc((void**)&dpart, sizeof(double) * 3 * pslots))) return rc;
     TG_CUDA(cudaMemsetAsync(dpart, 0, sizeof(double) * 3 * pslots, st), "memset");
     blocks = (int)std::min<long long>(((long long)g.M * g.M * g.Hk + 255) / 256, 2048);

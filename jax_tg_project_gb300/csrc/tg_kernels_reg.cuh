@@ -599,7 +599,14 @@ struct KxRegShape {
   static constexpr long long stage_elems = 2LL * 3 * MMAX * QW;
   static constexpr long long smem =
       (long long)sizeof(cplx<R>) * (N + (long long)NG * QW * CS + (long long)NG * stage_elems);
+  // adjoint kernels, per group: a ring of four [N][QW] input tiles of the forward transforms,
+  // or up to two [3][M][QW] spectral tiles, both staged by cp.async
+  static constexpr long long ring_elems = 4LL * N * QW;
+  static constexpr long long adj_area = (ring_elems > stage_elems) ? ring_elems : stage_elems;
+  static constexpr long long smem_adj =
+      (long long)sizeof(cplx<R>) * (N + (long long)NG * QW * CS + (long long)NG * adj_area);
 };
+
 
 
 
@@ -823,16 +830,80 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
   const int grp = threadIdx.x / GT, lt = threadIdx.x % GT;
   const int col = lt % QW, t = lt / QW;
   const int iyc = blockIdx.x, run = blockIdx.z;
-  const int kz = (blockIdx.y * Sh::NG + grp) * QW + col;
+  const int kz0 = (blockIdx.y * Sh::NG + grp) * QW;
+  const int kz = kz0 + col;
   const bool zok = kz < g.Hk;
   C* xcol = tw + N + (grp * QW + col) * CS;
+  C* stg = tw + N + Sh::NG * QW * CS + grp * Sh::adj_area;  // this group's staging area
+  // a group's barrier (its named barrier, or the warp when the group fits in one)
+  auto gsync = [&]() {
+    if constexpr (GT > 32) {
+      const NamedSync ns{1 + grp, GT};
+      ns();
+    } else {
+      __syncwarp();
+    }
+  };
+  // cp.async staging: rows of QW consecutive kz are 32-byte aligned (Hz % 4 == 0) and lie
+  // inside the padded rows (kz0 + QW <= Hz) whenever kz0 < Hk; a group without a valid
+  // column copies nothing but still commits, so that the group counts stay uniform
+  const bool gok = kz0 < g.Hk;
+  // forward input f (rows x = 0..N-1 of the X-layout field at src) -> ring slot f % 4
+  auto stage_x = [&](int f, const C* src) {
+    C* d = stg + (f & 3) * N * QW;
+    if (gok) {
+      for (int c = lt; c < 2 * N; c += GT) {
+        const int half = c & 1, row = c >> 1;
+        cp_async16(d + row * QW + 2 * half, src + (long long)row * M * Hz + 2 * half);
+      }
+    }
+    cp_async_commit();
+  };
+  // three spectral fields (rows (f, ic) of the compact layout at src) -> dst [3][M][QW]
+  auto stage_spec = [&](C* dst, const C* src) {
+    if (gok) {
+      for (int c = lt; c < 3 * M * 2; c += GT) {
+        const int half = c & 1, row = c >> 1;  // row = f * M + ic
+        cp_async16(dst + row * QW + 2 * half, src + (long long)row * M * Hz + 2 * half);
+      }
+    }
+  };
+  const long long soff0 = (long long)run * 3 * g.sS + (long long)iyc * Hz + kz0;
+  const int st = a.stage;
+  const C* const* tape = a.tp;
+  // the state whose u, curl u the load part transforms: spec_in, or the tape's stage state
+  // a_st, formed from V (tp[0]) and n_{st-1}
+  auto stage_state = [&]() {
+    if constexpr (TAPE) {
+      stage_spec(stg, tape[0] + soff0);
+      if (st > 1) stage_spec(stg + 3 * M * QW, tape[st - 1] + soff0);
+    } else {
+      stage_spec(stg, a.spec_in + soff0);
+    }
+    cp_async_commit();
+  };
+  // the first copies are issued before the twiddles are built
+  if constexpr (MODE == KX_NL_FWD) {
+    const C* win = a.in + (long long)run * 3 * g.sX + (long long)iyc * Hz + kz0;
+    for (int f = 0; f < 3; ++f) stage_x(f, win + f * g.sX);
+  } else if constexpr (HAS_FWD) {
+    const C* win = a.in + (long long)run * 6 * g.sX + (long long)iyc * Hz + kz0;
+    for (int f = 0; f < 4; ++f) stage_x(f, win + f * g.sX);
+  } else {
+    if (a.nout != 6) {  // mu = cl L + cg g_{st+1}: L (S) and, below stage 4, g (acc)
+      stage_spec(stg, a.S + soff0);
+      if (TAPE && st != 4) stage_spec(stg + 3 * M * QW, a.acc + soff0);
+      cp_async_commit();
+    } else {
+      stage_state();
+    }
+  }
   build_twiddles<Plan>(tw, a.tw, threadIdx.x, Sh::NT);
   __syncthreads();
   const float kyf = float(ksigned(iyc, K)), kzf = float(kz);
-  const long long soff = (long long)run * 3 * g.sS + (long long)iyc * Hz + kz;
+  const long long soff = soff0 + col;
   const RunCoef cf = a.coef[run];
   const R h = R(cf.dt);
-  const int st = a.stage;
   auto run_fft = [&](auto& src, auto& dst, auto dir_tag) {
     constexpr int DIR = decltype(dir_tag)::value;
     if constexpr (GT > 32) {
@@ -863,12 +934,15 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
   };
 
   if constexpr (MODE == KX_NL_FWD) {  // spec_out = P F(u x omega) / N^3 (nonlinear term alone)
-    const C* win = a.in + (long long)run * 3 * g.sX + (long long)iyc * Hz + kz;
     C nv[3][E];
 #pragma unroll
     for (int f = 0; f < 3; ++f) {
-      const C* wf = win + f * g.sX;
-      auto src = [&](int xx, int) -> C { return zok ? wf[(long long)xx * M * Hz] : czero<C>(); };
+      if (f == 0) cp_async_wait<2>();
+      else if (f == 1) cp_async_wait<1>();
+      else cp_async_wait_all();
+      gsync();
+      const C* sl = stg + f * N * QW + col;
+      auto src = [&](int xx, int) -> C { return zok ? sl[xx * QW] : czero<C>(); };
       auto dst = [&](int b, int r, int, C val) { nv[f][b + r * NBL] = cscale(val, inv_n3); };
       run_fft(src, dst, Fwd());
     }
@@ -888,12 +962,24 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
   C acc[3][E];  // g_s (forward part) or mu (projected, load part)
   if constexpr (HAS_FWD) {
     C z[E];
-    const C* win = a.in + (long long)run * 6 * g.sX + (long long)iyc * Hz + kz;
+    const C* win = a.in + (long long)run * 6 * g.sX + (long long)iyc * Hz + kz0;
+    // inputs 0..3 were issued at entry; 4 and 5 reuse the ring slots of 0 and 1 once their
+    // transforms are done.  Commit order 0 1 2 3 4 5, so before transform f the copies of
+    // f + 1 .. min(f + 3, 5) may still be in flight.
     auto fwd_to = [&](int f, auto* dstarr) {
-      const C* wf = win + f * g.sX;
-      auto src = [&](int xx, int) -> C { return zok ? wf[(long long)xx * M * Hz] : czero<C>(); };
+      if (f <= 2) cp_async_wait<3>();
+      else if (f == 3) cp_async_wait<2>();
+      else if (f == 4) cp_async_wait<1>();
+      else cp_async_wait_all();
+      gsync();
+      const C* sl = stg + (f & 3) * N * QW + col;
+      auto src = [&](int xx, int) -> C { return zok ? sl[xx * QW] : czero<C>(); };
       auto dst = [&](int b, int r, int, C val) { dstarr[b + r * NBL] = cscale(val, inv_n3); };
       run_fft(src, dst, Fwd());
+      if (f <= 1) {  // slot f is free once every thread of the group is past the transform
+        gsync();
+        stage_x(f + 4, win + (f + 4) * g.sX);
+      }
     };
     fwd_to(0, acc[0]);
     fwd_to(1, acc[1]);
@@ -929,59 +1015,92 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
       add_curl(std::integral_constant<int, 2>());
     }
     double dsum = 0.0;
+    if constexpr (!TAPE) {
 #pragma unroll
-    for (int q = 0; q < E; ++q) {
-      const int ic = kcompact_slot<N, P>(t, q, K);
-      if (zok && ic >= 0) {
-        if constexpr (!TAPE) {
+      for (int q = 0; q < E; ++q) {
+        const int ic = kcompact_slot<N, P>(t, q, K);
+        if (zok && ic >= 0) {
 #pragma unroll
           for (int f = 0; f < 3; ++f) a.spec_out[soff + ((long long)f * M + ic) * M * Hz] = acc[f][q];
-        } else {
-          R kk, m1, mh;
-          factors(ic, kk, m1, mh);
-          const R e1 = R(1) + m1, eh = R(1) + mh;
-          R dn = R(0);
+        }
+      }
+    } else {
+      // the stage is a compile-time constant inside (no branches between the loads), the
+      // buffers are distinct (restrict), and each mode's loads are issued before its
+      // arithmetic, so that the loads of several modes are in flight together
+      auto epilogue = [&](auto st_tag) {
+        constexpr int S = decltype(st_tag)::value;
+        const C* __restrict__ Lp = a.S;
+        const C* __restrict__ t0 = a.tp[0];
+        const C* __restrict__ t1 = a.tp[1];
+        const C* __restrict__ t2 = a.tp[2];
+        const C* __restrict__ t3 = a.tp[3];
+        C* __restrict__ lamp = a.vs;
+        C* __restrict__ gout = a.spec_out;
 #pragma unroll
-          for (int f = 0; f < 3; ++f) {
-            const long long o = soff + ((long long)f * M + ic) * M * Hz;
-            const C gs = acc[f][q];
-            if (a.spec_out != nullptr) a.spec_out[o] = gs;
-            C lam;
-            C l = czero<C>();  // L is read at stage 4 only (lam seed and its nu term)
-            if (st == 4) l = a.S[o];
-            if (st == 4) {
-              lam = mk<C>(e1 * (l.x + gs.x), e1 * (l.y + gs.y));
-            } else {
-              const R c = (st == 1) ? R(1) : eh;
-              lam = a.vs[o];
-              lam = mk<C>(lam.x + c * gs.x, lam.y + c * gs.y);
+        for (int q = 0; q < E; ++q) {
+          const int ic = kcompact_slot<N, P>(t, q, K);
+          if (zok && ic >= 0) {
+            long long o[3];
+            C l[3], v[3], y1[3], y2[3], y3[3];
+#pragma unroll
+            for (int f = 0; f < 3; ++f) {
+              o[f] = soff + ((long long)f * M + ic) * M * Hz;
+              l[f] = (S == 4) ? Lp[o[f]] : lamp[o[f]];  // L at stage 4, else the lam so far
+              if constexpr (S >= 2) v[f] = t0[o[f]];
+              if constexpr (S == 4 || S == 2) y1[f] = t1[o[f]];
+              if constexpr (S == 4) {
+                y2[f] = t2[o[f]];
+                y3[f] = t3[o[f]];
+              }
             }
-            a.vs[o] = lam;
-            if (st >= 2) {
-              const C v = a.tp[0][o];
-              if (st == 4) {
-                const C y1 = a.tp[1][o], y2 = a.tp[2][o], y3 = a.tp[3][o];
-                const R b4x = -kk * h * e1 * v.x - kk * R(0.5) * h * h * eh * y3.x;
-                const R b4y = -kk * h * e1 * v.y - kk * R(0.5) * h * h * eh * y3.y;
-                const R bLx = -kk * h * e1 * v.x - kk * h * h / R(6) * (e1 * y1.x + eh * (y2.x + y3.x));
-                const R bLy = -kk * h * e1 * v.y - kk * h * h / R(6) * (e1 * y1.y + eh * (y2.y + y3.y));
-                dn += gs.x * b4x + gs.y * b4y + l.x * bLx + l.y * bLy;
-              } else if (st == 3) {
-                const R c3 = -kk * R(0.5) * h * eh;
-                dn += c3 * (gs.x * v.x + gs.y * v.y);
+            R kk, m1, mh;
+            factors(ic, kk, m1, mh);
+            const R e1 = R(1) + m1, eh = R(1) + mh;
+            R dn = R(0);
+#pragma unroll
+            for (int f = 0; f < 3; ++f) {
+              const C gs = acc[f][q];
+              if (gout != nullptr) gout[o[f]] = gs;
+              C lam;
+              if constexpr (S == 4) {
+                lam = mk<C>(e1 * (l[f].x + gs.x), e1 * (l[f].y + gs.y));
               } else {
-                const C y1 = a.tp[1][o];
-                const R a2x = v.x + (mh * v.x + eh * R(0.5) * h * y1.x);
-                const R a2y = v.y + (mh * v.y + eh * R(0.5) * h * y1.y);
+                const R c = (S == 1) ? R(1) : eh;
+                lam = mk<C>(l[f].x + c * gs.x, l[f].y + c * gs.y);
+              }
+              lamp[o[f]] = lam;
+              if constexpr (S == 4) {
+                const C vv = v[f], a1 = y1[f], a2 = y2[f], a3 = y3[f], ll = l[f];
+                const R b4x = -kk * h * e1 * vv.x - kk * R(0.5) * h * h * eh * a3.x;
+                const R b4y = -kk * h * e1 * vv.y - kk * R(0.5) * h * h * eh * a3.y;
+                const R bLx = -kk * h * e1 * vv.x - kk * h * h / R(6) * (e1 * a1.x + eh * (a2.x + a3.x));
+                const R bLy = -kk * h * e1 * vv.y - kk * h * h / R(6) * (e1 * a1.y + eh * (a2.y + a3.y));
+                dn += gs.x * b4x + gs.y * b4y + ll.x * bLx + ll.y * bLy;
+              } else if constexpr (S == 3) {
+                const R c3 = -kk * R(0.5) * h * eh;
+                dn += c3 * (gs.x * v[f].x + gs.y * v[f].y);
+              } else if constexpr (S == 2) {
+                const C vv = v[f], a1 = y1[f];
+                const R a2x = vv.x + (mh * vv.x + eh * R(0.5) * h * a1.x);
+                const R a2y = vv.y + (mh * vv.y + eh * R(0.5) * h * a1.y);
                 dn += -kk * R(0.5) * h * (gs.x * a2x + gs.y * a2y);
               }
             }
+            dsum += (kz == 0 ? 1.0 : 2.0) * double(dn);
           }
-          dsum += (kz == 0 ? 1.0 : 2.0) * double(dn);
         }
+      };
+      switch (st) {
+        case 4: epilogue(std::integral_constant<int, 4>()); break;
+        case 3: epilogue(std::integral_constant<int, 3>()); break;
+        case 2: epilogue(std::integral_constant<int, 2>()); break;
+        default: epilogue(std::integral_constant<int, 1>()); break;
       }
     }
     if constexpr (TAPE) {
+      // the host allocates M x ceil(Hk / 4) partial-sum slots per stage
+      static_assert(QW == 4, "partial-sum slots assume four kz columns per group");
       if (st >= 2 && a.part != nullptr) {  // CTA sum in a fixed order: warp tree, then the warps
         __shared__ double wsum[Sh::NT / 32];
         for (int o = 16; o > 0; o >>= 1) dsum += __shfl_down_sync(0xffffffffu, dsum, o);
@@ -1001,7 +1120,6 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
     // state: one three-field array live at a time.  nout = 9 writes u, omega into out and a
     // into out2 (tape forms) or into out's fields 6..8; nout = 3 only a, nout = 6 only u, omega.
     const int sl = st;  // load stage
-    const C* const* tape = a.tp;
     C* xo = a.out + (long long)run * a.nout * g.sX + (long long)iyc * Hz + kz;
     const int gi0 = (a.nout == 3) ? 6 : 0;  // output field of GI = gi0 + slot
     C* xa = (TAPE && a.nout == 9) ? a.out2 + (long long)iyc * Hz + kz - 6 * g.sX : xo - gi0 * g.sX;
@@ -1037,6 +1155,10 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
       };
       run_fft(src, dst, Inv());
     };
+    if (a.nout != 6) {  // the staged L (and g) tiles
+      cp_async_wait_all();
+      gsync();
+    }
     {  // mu (projected) into acc: plain S, or the tape seeds
 #pragma unroll
       for (int q = 0; q < E; ++q) {
@@ -1050,13 +1172,12 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
         }
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
-          const long long o = soff + ((long long)f * M + (ok ? ic : 0)) * M * Hz;
           C m = czero<C>();
           if (ok && a.nout != 6) {
-            const C l = a.S[o];
+            const C l = stg[((long long)f * M + ic) * QW + col];
             m = mk<C>(cl * l.x, cl * l.y);
             if (TAPE && sl != 4) {
-              const C gp = a.acc[o];
+              const C gp = stg[((long long)(3 + f) * M + ic) * QW + col];
               m = mk<C>(m.x + cg * gp.x, m.y + cg * gp.y);
             }
           }
@@ -1069,6 +1190,10 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
       }
     }
     if (a.nout != 6) {
+      if (a.nout != 3) {  // the tiles of mu are consumed: stage the state during a's transforms
+        gsync();
+        stage_state();
+      }
       if constexpr (N >= 128) {
 #pragma unroll 1
         for (int gi = 6; gi < 9; ++gi) field(gi, acc);
@@ -1079,6 +1204,8 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
     }
     if (a.nout != 3) {
       // the state whose u, curl u are transformed: spec_in, or the tape's stage state a_sl
+      cp_async_wait_all();
+      gsync();
       C v[3][E];
 #pragma unroll
       for (int q = 0; q < E; ++q) {
@@ -1089,12 +1216,11 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
         const R eh = R(1) + mh;
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
-          const long long o = soff + ((long long)f * M + (ok ? ic : 0)) * M * Hz;
           C x = czero<C>();
           if (ok) {
-            x = TAPE ? tape[0][o] : a.spec_in[o];
+            x = stg[((long long)f * M + ic) * QW + col];
             if (TAPE && sl > 1) {
-              const C nn = tape[sl - 1][o];
+              const C nn = stg[((long long)(3 + f) * M + ic) * QW + col];
               R dx, dy;
               if (sl == 2) { dx = mh * x.x + eh * R(0.5) * h * nn.x; dy = mh * x.y + eh * R(0.5) * h * nn.y; }
               else if (sl == 3) { dx = mh * x.x + R(0.5) * h * nn.x; dy = mh * x.y + R(0.5) * h * nn.y; }
@@ -1119,11 +1245,11 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
 template <typename R, int N, int MODE>
 static cudaError_t launch_kx_reg_adj(const PassArgs<R>& a, int runs, cudaStream_t st) {
   using Sh = KxRegShape<R, N>;
-  static cudaError_t attr = set_smem(kx_reg_adj_kernel<R, N, MODE>, Sh::smem);
+  static cudaError_t attr = set_smem(kx_reg_adj_kernel<R, N, MODE>, Sh::smem_adj);
   if (attr != cudaSuccess) return attr;
   const int quads = (a.g.Hk + Sh::QW - 1) / Sh::QW;
   dim3 grid(a.g.M, (quads + Sh::NG - 1) / Sh::NG, runs);
-  kx_reg_adj_kernel<R, N, MODE><<<grid, Sh::NT, Sh::smem, st>>>(a);
+  kx_reg_adj_kernel<R, N, MODE><<<grid, Sh::NT, Sh::smem_adj, st>>>(a);
   return cudaGetLastError();
 }
 
