@@ -585,7 +585,11 @@ template <typename R, int N>
 struct KxRegShape {
   using Plan = typename RegPlan<N>::T;
   static constexpr int P = Plan::P, E = Plan::E;
-  static constexpr int QW = 4;                      // kz columns per group (one 32-byte sector)
+  // kz columns per group (one 32-byte sector; 8-column groups at 256, with a conflict-free
+  // exchange stride = 2 (mod 16), measured no faster).  The staging loops copy 16-byte chunks
+  // and skip any past the padded row (Hz is a multiple of 4), whose columns are never used.
+  static constexpr int QW = 4;
+  static constexpr int CPR = QW / 2;                // 16-byte cp.async chunks per row segment
   static constexpr int GT = QW * P;                 // threads per group
   static constexpr int TARGET = (P >= 16) ? 256 : 128;  // threads per CTA
   static constexpr int NG = (GT >= TARGET) ? 1 : TARGET / GT;
@@ -593,7 +597,8 @@ struct KxRegShape {
   // resident CTAs per SM the registers must allow (E = 12 at N = 96 needs ~168 registers)
   static constexpr int MINB = (NT >= 256) ? 2 : ((E > 8) ? 3 : 4);
   static constexpr int PSH = 3;
-  static constexpr int CS = ColLayout<N, PSH, 4>::CS;
+  // exchange column stride: = 4 (mod 16) for 4-column groups, = 2 for 8 (bank-conflict model)
+  static constexpr int CS = ColLayout<N, PSH, (QW == 8) ? 2 : 4>::CS;
   static constexpr int MMAX = 2 * (N / 3) + 1;
   // per group: state and accumulator tiles [2][3][M][QW], staged by cp.async
   static constexpr long long stage_elems = 2LL * 3 * MMAX * QW;
@@ -642,17 +647,19 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
   C* stg = tw + N + Sh::NG * QW * CS + grp * Sh::stage_elems;
   if constexpr (MODE == KX_STAGE) {
     // stage the state (and accumulator) tiles of this group while the forward
-    // transforms run: rows of QW consecutive kz are 32-byte aligned (Hz % 4 == 0)
-    // and lie inside the padded rows (kz0 + QW <= Hz) whenever kz0 < Hk
+    // transforms run: rows of QW consecutive kz are 32-byte aligned (Hz % 4 == 0, kz0 a
+    // multiple of QW); chunks past the padded row (kz0 + 2h >= Hz) are skipped
     if (kz0 < g.Hk) {
       const int narr = (a.stage > 1) ? 2 : 1;
       const long long base = (long long)blockIdx.z * 3 * g.sS + (long long)iyc * Hz + kz0;
-      const int chunks = narr * 3 * M * 2;  // 16-byte halves of each 32-byte row
+      constexpr int CPR = Sh::CPR;
+      const int chunks = narr * 3 * M * CPR;  // 16-byte chunks of each row segment
       for (int c = lt; c < chunks; c += GT) {
-        const int half = c & 1, row = c >> 1;  // row = (arr * 3 + f) * M + ic
+        const int h = c % CPR, row = c / CPR;  // row = (arr * 3 + f) * M + ic
+        if (kz0 + 2 * h >= Hz) continue;
         const int arr = row / (3 * M), fi = row % (3 * M);
-        const C* src = (arr == 0 ? a.S : a.acc) + base + (long long)fi * M * Hz + 2 * half;
-        cp_async16(stg + (long long)row * QW + 2 * half, src);
+        const C* src = (arr == 0 ? a.S : a.acc) + base + (long long)fi * M * Hz + 2 * h;
+        cp_async16(stg + (long long)row * QW + 2 * h, src);
       }
     }
     cp_async_commit();
@@ -844,17 +851,17 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
       __syncwarp();
     }
   };
-  // cp.async staging: rows of QW consecutive kz are 32-byte aligned (Hz % 4 == 0) and lie
-  // inside the padded rows (kz0 + QW <= Hz) whenever kz0 < Hk; a group without a valid
+  // cp.async staging: rows of QW consecutive kz are 32-byte aligned (Hz % 4 == 0); chunks
+  // past the padded row (kz0 + 2h >= Hz) are skipped; a group without a valid
   // column copies nothing but still commits, so that the group counts stay uniform
   const bool gok = kz0 < g.Hk;
   // forward input f (rows x = 0..N-1 of the X-layout field at src) -> ring slot f % 4
   auto stage_x = [&](int f, const C* src) {
     C* d = stg + (f & 3) * N * QW;
     if (gok) {
-      for (int c = lt; c < 2 * N; c += GT) {
-        const int half = c & 1, row = c >> 1;
-        cp_async16(d + row * QW + 2 * half, src + (long long)row * M * Hz + 2 * half);
+      for (int c = lt; c < Sh::CPR * N; c += GT) {
+        const int h = c % Sh::CPR, row = c / Sh::CPR;
+        if (kz0 + 2 * h < Hz) cp_async16(d + row * QW + 2 * h, src + (long long)row * M * Hz + 2 * h);
       }
     }
     cp_async_commit();
@@ -862,9 +869,9 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
   // three spectral fields (rows (f, ic) of the compact layout at src) -> dst [3][M][QW]
   auto stage_spec = [&](C* dst, const C* src) {
     if (gok) {
-      for (int c = lt; c < 3 * M * 2; c += GT) {
-        const int half = c & 1, row = c >> 1;  // row = f * M + ic
-        cp_async16(dst + row * QW + 2 * half, src + (long long)row * M * Hz + 2 * half);
+      for (int c = lt; c < 3 * M * Sh::CPR; c += GT) {
+        const int h = c % Sh::CPR, row = c / Sh::CPR;  // row = f * M + ic
+        if (kz0 + 2 * h < Hz) cp_async16(dst + row * QW + 2 * h, src + (long long)row * M * Hz + 2 * h);
       }
     }
   };
@@ -1100,7 +1107,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
     }
     if constexpr (TAPE) {
       // the host allocates M x ceil(Hk / 4) partial-sum slots per stage
-      static_assert(QW == 4, "partial-sum slots assume four kz columns per group");
+      static_assert(QW % 4 == 0, "partial-sum slots assume at least four kz columns per group");
       if (st >= 2 && a.part != nullptr) {  // CTA sum in a fixed order: warp tree, then the warps
         __shared__ double wsum[Sh::NT / 32];
         for (int o = 16; o > 0; o >>= 1) dsum += __shfl_down_sync(0xffffffffu, dsum, o);
