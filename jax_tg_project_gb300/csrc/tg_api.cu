@@ -56,9 +56,16 @@ static LaunchFn<double> find_f64(int n) {
 }
 
 // ------------------------------------------------------------------ generic kernels
-constexpr int kDiagBlocks = 96;
+constexpr int kDiagBlocks = 304;  // at most two CTAs per SM
 constexpr int kDiagThreads = 256;
 constexpr int kNQ = 5;  // E_k, enstrophy, sum w k^2 |u|^2, E_m, H_c
+
+// CTAs of diag_partial for a grid: one (kx, ky) row of the compact spectrum per warp and
+// pass, at most kDiagBlocks
+static int diag_blocks(const Geo& g) {
+  const long long rows = (long long)g.M * g.M;
+  return (int)std::min<long long>(kDiagBlocks, (rows + kDiagThreads / 32 - 1) / (kDiagThreads / 32));
+}
 
 struct Neumaier {
   double s = 0.0, c = 0.0;
@@ -70,44 +77,29 @@ struct Neumaier {
   __device__ __forceinline__ double value() const { return s + c; }
 };
 
+// per-CTA partial sums of the five diagnostic terms: each warp takes whole (kx, ky) rows
+// (lanes along kz), each thread sums its own modes in FP64 in a fixed order, then a fixed
+// tree over the CTA
 template <typename R>
 __global__ void __launch_bounds__(kDiagThreads) diag_partial(const cplx<R>* S, Geo g, int F, double* part) {
   using C = cplx<R>;
   const int run = blockIdx.y;
   const C* base = S + (long long)run * F * g.sS;
-  const long long total = (long long)g.M * g.M * g.Hk;
-  Neumaier q[kNQ];
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int kz = int(idx % g.Hk);
-    const long long r = idx / g.Hk;
-    const int iyc = int(r % g.M), ic = int(r / g.M);
-    const double kx = ksigned(ic, g.K), ky = ksigned(iyc, g.K), kzd = kz;
-    const double w = (kz == 0) ? 1.0 : 2.0;
-    const long long o = ((long long)ic * g.M + iyc) * g.Hz + kz;
-    const C ux = base[o], uy = base[g.sS + o], uz = base[2 * g.sS + o];
-    const double e2 = double(ux.x) * ux.x + double(ux.y) * ux.y + double(uy.x) * uy.x +
-                      double(uy.y) * uy.y + double(uz.x) * uz.x + double(uz.y) * uz.y;
-    // |k x u|^2 with complex components
-    const double cxr = ky * uz.x - kzd * uy.x, cxi = ky * uz.y - kzd * uy.y;
-    const double cyr = kzd * ux.x - kx * uz.x, cyi = kzd * ux.y - kx * uz.y;
-    const double czr = kx * uy.x - ky * ux.x, czi = kx * uy.y - ky * ux.y;
-    const double c2 = cxr * cxr + cxi * cxi + cyr * cyr + cyi * cyi + czr * czr + czi * czi;
-    q[0].add(0.5 * w * e2);
-    q[1].add(0.5 * w * c2);
-    q[2].add(w * (kx * kx + ky * ky + kzd * kzd) * e2);
-    if (F == 6) {
-      const C bx = base[3 * g.sS + o], by = base[4 * g.sS + o], bz = base[5 * g.sS + o];
-      const double b2 = double(bx.x) * bx.x + double(bx.y) * bx.y + double(by.x) * by.x +
-                        double(by.y) * by.y + double(bz.x) * bz.x + double(bz.y) * bz.y;
-      const double hc = double(ux.x) * bx.x + double(ux.y) * bx.y + double(uy.x) * by.x +
-                        double(uy.y) * by.y + double(uz.x) * bz.x + double(uz.y) * bz.y;
-      q[3].add(0.5 * w * b2);
-      q[4].add(w * hc);
+  const int lane = threadIdx.x & 31;
+  const int nw = kDiagThreads / 32;
+  double q[kNQ] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int r = blockIdx.x * nw + (threadIdx.x >> 5); r < g.M * g.M; r += gridDim.x * nw) {
+    const int ic = r / g.M, iyc = r - ic * g.M;
+    const int kx = ksigned(ic, g.K), ky = ksigned(iyc, g.K);
+    for (int kz = lane; kz < g.Hk; kz += 32) {
+      double t[kNQ];
+      diag_terms(base, g.sS, (long long)r * g.Hz + kz, kx, ky, kz, F, t);
+#pragma unroll
+      for (int i = 0; i < kNQ; ++i) q[i] += t[i];
     }
   }
   __shared__ double sh[kNQ][kDiagThreads];
-  for (int i = 0; i < kNQ; ++i) sh[i][threadIdx.x] = q[i].value();
+  for (int i = 0; i < kNQ; ++i) sh[i][threadIdx.x] = q[i];
   __syncthreads();
   for (int s = kDiagThreads / 2; s > 0; s >>= 1) {
     if (threadIdx.x < s)
@@ -117,16 +109,19 @@ __global__ void __launch_bounds__(kDiagThreads) diag_partial(const cplx<R>* S, G
   if (threadIdx.x < kNQ) part[((long long)run * gridDim.x + blockIdx.x) * kNQ + threadIdx.x] = sh[threadIdx.x][0];
 }
 
-// one block per run: fixed-order compensated sum of the partials, one record
-__global__ void diag_final(const double* part, int nblk, const RunCoef* coef, const unsigned long long* amax,
-                           int namax, int F, double* out) {
+// one CTA of kNQ warps per run: warp i sums quantity i over the nblk partials (lane l takes
+// partials l, l + 32, ... with compensation, then a fixed shuffle tree), one record
+__global__ void __launch_bounds__(32 * kNQ) diag_final(const double* part, int nblk, const RunCoef* coef,
+                                                       const unsigned long long* amax, int namax, int F,
+                                                       double* out) {
   const int run = blockIdx.x;
+  const int i = threadIdx.x >> 5, lane = threadIdx.x & 31;
   __shared__ double v[kNQ];
-  if (threadIdx.x < kNQ) {
-    Neumaier s;
-    for (int b = 0; b < nblk; ++b) s.add(part[((long long)run * nblk + b) * kNQ + threadIdx.x]);
-    v[threadIdx.x] = s.value();
-  }
+  Neumaier s;
+  for (int b = lane; b < nblk; b += 32) s.add(part[((long long)run * nblk + b) * kNQ + i]);
+  double x = s.value();
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  if (lane == 0) v[i] = x;
   __syncthreads();
   if (threadIdx.x == 0) {
     double* o = out + (long long)run * TG_DIAG_WIDTH;
@@ -576,15 +571,10 @@ __global__ void __launch_bounds__(256) spectrum_partial(const cplx<R>* S, Geo g,
         const int bin = int(floor(sqrt(kx * kx + ky * ky + double(kz) * kz) + 0.5));
         const double w = (kz == 0) ? 1.0 : 2.0;
         const long long o = ((long long)ic * g.M + iyc) * g.Hz + kz;
-        double eu = 0.0, eb = 0.0;
-        for (int f = 0; f < 3; ++f) {
-          const cplx<R> v = base[f * g.sS + o];
-          eu += double(v.x) * v.x + double(v.y) * v.y;
-          if (F == 6) {
-            const cplx<R> b = base[(3 + f) * g.sS + o];
-            eb += double(b.x) * b.x + double(b.y) * b.y;
-          }
-        }
+        // the per-mode squares of the scalar diagnostics (mode_sq), so that the bins sum
+        // to their energies
+        const double eu = double(mode_sq(base[o], base[g.sS + o], base[2 * g.sS + o]));
+        const double eb = (F == 6) ? double(mode_sq(base[3 * g.sS + o], base[4 * g.sS + o], base[5 * g.sS + o])) : 0.0;
         if (bin < nbins) {
           hist[bin] += 0.5 * w * eu;
           hist[nbins + bin] += 0.5 * w * eb;
@@ -802,10 +792,11 @@ struct Ops {
       a.flags |= FLAG_AMAX;
       if ((rc = go(p, OP_KZ_C2R, a, "kz divergence"))) return rc;
     }
-    dim3 grid(kDiagBlocks, p->batch);
+    const int nblk = diag_blocks(p->g);
+    dim3 grid(nblk, p->batch);
     diag_partial<R><<<grid, kDiagThreads, 0, p->st>>>(static_cast<const C*>(S), p->g, p->F, p->part);
     TG_CUDA(cudaGetLastError(), "diag_partial");
-    diag_final<<<p->batch, 32, 0, p->st>>>(p->part, kDiagBlocks, p->coef, p->amax, nd, p->F, out);
+    diag_final<<<p->batch, 32 * kNQ, 0, p->st>>>(p->part, nblk, p->coef, p->amax, nd, p->F, out);
     TG_CUDA(cudaGetLastError(), "diag_final");
     p->launches += 2;
     return TG_OK;
@@ -868,9 +859,10 @@ struct Ops {
       pert_kernel<R><<<(int)std::min<long long>((modes + 255) / 256, 4096), 256, 0, p->st>>>(
           P, p->g, p->batch, (unsigned long long)seed, k0);
       TG_CUDA(cudaGetLastError(), "pert_kernel");
-      dim3 grid(kDiagBlocks, p->batch);
+      const int nblk = diag_blocks(p->g);
+      dim3 grid(nblk, p->batch);
       diag_partial<R><<<grid, kDiagThreads, 0, p->st>>>(P, p->g, 3, p->part);
-      diag_final<<<p->batch, 32, 0, p->st>>>(p->part, kDiagBlocks, p->coef, p->amax, 0, 3, p->dtmp);
+      diag_final<<<p->batch, 32 * kNQ, 0, p->st>>>(p->part, nblk, p->coef, p->amax, 0, 3, p->dtmp);
       TG_CUDA(cudaGetLastError(), "perturbation energy");
       std::vector<double> rec((size_t)p->batch * TG_DIAG_WIDTH), scale(p->batch);
       TG_CUDA(cudaMemcpyAsync(rec.data(), p->dtmp, rec.size() * sizeof(double), cudaMemcpyDeviceToHost, p->st),

@@ -120,6 +120,63 @@ __device__ __forceinline__ int kcompact(int k, int N, int K) {
 // full-axis frequency row of compact index i
 __device__ __forceinline__ int kfull(int i, int N, int K) { return i <= K ? i : i + N - (2 * K + 1); }
 
+// Per-mode terms of the scalar diagnostics and the energy spectrum.  For FP32 states the
+// products and their six-term sums are formed in FP32 (the precision the state itself
+// carries, ~1e-7 relative per term) and widened to FP64 for accumulation; FP64 states use
+// FP64 throughout.  The diagnostics, the allocation-free diagnostics and the spectrum share
+// these, so that their per-mode terms agree bit for bit.
+__device__ __forceinline__ float mode_sq(float2 a, float2 b, float2 c) {  // |a|^2 + |b|^2 + |c|^2
+  float s = a.x * a.x;
+  s = fmaf(a.y, a.y, s);
+  s = fmaf(b.x, b.x, s);
+  s = fmaf(b.y, b.y, s);
+  s = fmaf(c.x, c.x, s);
+  return fmaf(c.y, c.y, s);
+}
+__device__ __forceinline__ double mode_sq(double2 a, double2 b, double2 c) {
+  return a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y + c.x * c.x + c.y * c.y;
+}
+__device__ __forceinline__ float mode_dot(float2 a, float2 b, float2 c, float2 p, float2 q, float2 r) {
+  float s = a.x * p.x;  // Re(a conj p + b conj q + c conj r)
+  s = fmaf(a.y, p.y, s);
+  s = fmaf(b.x, q.x, s);
+  s = fmaf(b.y, q.y, s);
+  s = fmaf(c.x, r.x, s);
+  return fmaf(c.y, r.y, s);
+}
+__device__ __forceinline__ double mode_dot(double2 a, double2 b, double2 c, double2 p, double2 q, double2 r) {
+  return a.x * p.x + a.y * p.y + b.x * q.x + b.y * q.y + c.x * r.x + c.y * r.y;
+}
+// |k x u|^2 with complex components (k integer-valued, exact in either precision)
+template <typename R, typename C>
+__device__ __forceinline__ R mode_curl_sq(R kx, R ky, R kz, C ux, C uy, C uz) {
+  const C cx = {ky * uz.x - kz * uy.x, ky * uz.y - kz * uy.y};
+  const C cy = {kz * ux.x - kx * uz.x, kz * ux.y - kx * uz.y};
+  const C cz = {kx * uy.x - ky * ux.x, kx * uy.y - ky * ux.y};
+  return mode_sq(cx, cy, cz);
+}
+// the five diagnostic terms of compact mode o (weight w = 1 at kz = 0, else 2):
+//   w/2 |u|^2, w/2 |k x u|^2, w |k|^2 |u|^2, and for F = 6 w/2 |b|^2, w Re(u . conj b)
+template <typename C>
+__device__ __forceinline__ void diag_terms(const C* base, long long sS, long long o, int kx, int ky, int kz,
+                                           int F, double t[5]) {
+  using R = decltype(C{}.x);
+  const R hw = (kz == 0) ? R(0.5) : R(1);  // w / 2
+  const R fx = R(kx), fy = R(ky), fz = R(kz);
+  const C ux = base[o], uy = base[sS + o], uz = base[2 * sS + o];
+  const R e2 = mode_sq(ux, uy, uz);
+  t[0] = double(hw * e2);  // exact scalings by powers of two
+  t[1] = double(hw * mode_curl_sq(fx, fy, fz, ux, uy, uz));
+  t[2] = double((R(2) * hw * R(kx * kx + ky * ky + kz * kz)) * e2);
+  if (F == 6) {
+    const C bx = base[3 * sS + o], by = base[4 * sS + o], bz = base[5 * sS + o];
+    t[3] = double(hw * mode_sq(bx, by, bz));
+    t[4] = double(R(2) * hw * mode_dot(ux, uy, uz, bx, by, bz));
+  } else {
+    t[3] = t[4] = 0.0;
+  }
+}
+
 // Slot q of a thread holds the modes k = t + P q (0 <= t < P).  Every dealiasing cutoff
 // satisfies K <= N/3, so a slot lying wholly inside (N/3, N - N/3) only ever holds removed
 // modes, and a slot with P q > N/3 never holds a kept non-negative kz: both tests are

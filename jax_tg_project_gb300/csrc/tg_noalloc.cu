@@ -56,35 +56,20 @@ __global__ void __launch_bounds__(kThreads) partial_kernel(const tg::cplx<R>* S,
   using C = tg::cplx<R>;
   const int run = blockIdx.y;
   const C* base = S + (long long)run * F * g.sS;
-  const long long total = (long long)g.M * g.M * g.Hk;
-  Comp q[kQ];
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int kz = int(idx % g.Hk);
-    const long long r = idx / g.Hk;
-    const int iy = int(r % g.M), ix = int(r / g.M);
-    const double kx = tg::ksigned(ix, g.K), ky = tg::ksigned(iy, g.K), kzd = kz;
-    const double w = (kz == 0) ? 1.0 : 2.0;
-    const long long o = ((long long)ix * g.M + iy) * g.Hz + kz;
-    const C ux = base[o], uy = base[g.sS + o], uz = base[2 * g.sS + o];
-    const double e2 = double(ux.x) * ux.x + double(ux.y) * ux.y + double(uy.x) * uy.x +
-                      double(uy.y) * uy.y + double(uz.x) * uz.x + double(uz.y) * uz.y;
-    const double cxr = ky * uz.x - kzd * uy.x, cxi = ky * uz.y - kzd * uy.y;
-    const double cyr = kzd * ux.x - kx * uz.x, cyi = kzd * ux.y - kx * uz.y;
-    const double czr = kx * uy.x - ky * ux.x, czi = kx * uy.y - ky * ux.y;
-    q[0].add(0.5 * w * e2);
-    q[1].add(0.5 * w * (cxr * cxr + cxi * cxi + cyr * cyr + cyi * cyi + czr * czr + czi * czi));
-    q[2].add(w * (kx * kx + ky * ky + kzd * kzd) * e2);
-    if (F == 6) {
-      const C bx = base[3 * g.sS + o], by = base[4 * g.sS + o], bz = base[5 * g.sS + o];
-      q[3].add(0.5 * w * (double(bx.x) * bx.x + double(bx.y) * bx.y + double(by.x) * by.x +
-                          double(by.y) * by.y + double(bz.x) * bz.x + double(bz.y) * bz.y));
-      q[4].add(w * (double(ux.x) * bx.x + double(ux.y) * bx.y + double(uy.x) * by.x +
-                    double(uy.y) * by.y + double(uz.x) * bz.x + double(uz.y) * bz.y));
+  // the per-mode terms of tg_diagnostics (diag_terms), one (kx, ky) row per warp and pass
+  double q[kQ] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  const int lane = threadIdx.x & 31, nw = kThreads / 32;
+  for (int r = blockIdx.x * nw + (threadIdx.x >> 5); r < g.M * g.M; r += gridDim.x * nw) {
+    const int ix = r / g.M, iy = r - ix * g.M;
+    const int kx = tg::ksigned(ix, g.K), ky = tg::ksigned(iy, g.K);
+    for (int kz = lane; kz < g.Hk; kz += 32) {
+      double t[kQ];
+      tg::diag_terms(base, g.sS, (long long)r * g.Hz + kz, kx, ky, kz, F, t);
+      for (int i = 0; i < kQ; ++i) q[i] += t[i];
     }
   }
   __shared__ double sh[kQ][kThreads];
-  for (int i = 0; i < kQ; ++i) sh[i][threadIdx.x] = q[i].value();
+  for (int i = 0; i < kQ; ++i) sh[i][threadIdx.x] = q[i];
   __syncthreads();
   for (int s = kThreads / 2; s > 0; s >>= 1) {
     if (threadIdx.x < s)
