@@ -696,18 +696,18 @@ struct Ops {
     return TG_OK;
   }
   // spectral state -> inverse-x of nout fields (map) into X
-  static int load_inv(tg_plan* p, const void* S, int map, int nin, int nout) {
+  static int load_inv(tg_plan* p, const void* S, int map, int nin, int nout, void* out = nullptr) {
     PassArgs<R> a = base(p);
     a.spec_in = static_cast<const C*>(S);
-    a.out = static_cast<C*>(p->X);
+    a.out = static_cast<C*>(out ? out : p->X);
     a.map = map;
     a.nin = nin;
     a.nout = nout;
     return go(p, p->F == 6 ? OP_KX_LOAD6 : OP_KX_LOAD3, a, "kx load");
   }
-  static int y_inv(tg_plan* p, int nf) {
+  static int y_inv(tg_plan* p, int nf, const void* in = nullptr) {
     PassArgs<R> a = base(p);
-    a.in = static_cast<const C*>(p->X);
+    a.in = static_cast<const C*>(in ? in : p->X);
     a.out = static_cast<C*>(p->Y);
     a.nin = a.nout = nf;
     return go(p, OP_KY_INV, a, "ky inverse");
@@ -781,8 +781,10 @@ struct Ops {
     int rc;
     const int nd = p->F / 3;
     TG_CUDA(cudaMemsetAsync(p->amax, 0, sizeof(unsigned long long) * p->batch * 2, p->st), "memset");
-    if ((rc = load_inv(p, S, MAP_DIV, p->F, nd))) return rc;
-    if ((rc = y_inv(p, nd))) return rc;
+    // the divergence goes through Z (x-pass layout, nd <= F fields) and Y, so that X keeps
+    // the inverse-x fields of a state being advanced (tg_run loads the state once)
+    if ((rc = load_inv(p, S, MAP_DIV, p->F, nd, p->Z))) return rc;
+    if ((rc = y_inv(p, nd, p->Z))) return rc;
     {
       PassArgs<R> a = base(p);
       a.in = static_cast<const C*>(p->Y);
@@ -1274,11 +1276,17 @@ int tg_run(tg_plan* p, void* state, double dt, double nu, double eta, int nsteps
   total += p->launches;
   int rec = 1;
   int step = 0;
-  while (step < nsteps) {
-    const int chunk = std::min(save_every - (step % save_every), nsteps - step);
+  // X holds the inverse-x fields of the state from here on: the steps leave those of their
+  // result, and the diagnostics between chunks do not use X
+  if (nsteps > 0) {
     p->launches = 0;
     rc = dispatch(p, [&](auto ops) { return decltype(ops)::start(p, state); });
     if (rc) return rc;
+    total += p->launches;
+  }
+  while (step < nsteps) {
+    const int chunk = std::min(save_every - (step % save_every), nsteps - step);
+    p->launches = 0;
     rc = advance(p, state, chunk);
     if (rc) return rc;
     step += chunk;

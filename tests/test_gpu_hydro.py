@@ -211,3 +211,22 @@ def test_512_transforms_and_early_steps_match_256():
     assert rel_l2(lo5, lo2) < 1e-5
     del p5, p2
     torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("physics", ["hydro", "mhd"])
+def test_run_in_chunks_matches_step(physics):
+    """Plan.run loads the state once and carries the inverse-x fields across its diagnostics
+    records (which go through other scratch): the final state equals Plan.step's bit for bit."""
+    import torch
+
+    import jax_tg_project_gb300 as tg
+    p = tg.Plan(32, physics=physics, precision="f32")
+    kind = "taylor_green" if physics == "hydro" else "mhd_equal_energy"
+    a = p.initial_condition(kind, seed=5, pert_amp=0.03, k0=3.0)
+    b = a.clone()
+    series = p.run(a, dt=2e-3, nu=0.004, eta=0.003, nsteps=7, save_every=3)
+    p.step(b, dt=2e-3, nu=0.004, eta=0.003, nsteps=7)
+    assert series.shape[0] == 4
+    assert torch.equal(a, b)
+    d = p.diagnostics(b, nu=0.004, eta=0.003)
+    assert torch.equal(series[-1], d)
