@@ -95,22 +95,12 @@ template <> __device__ __forceinline__ double rexpm1<double>(double x) { return 
 // form s + expm1(-lin t) s: for the small lin*h of a DNS step, E rounded to the
 // working precision would bias the viscous decay (e.g. 1 - 1.9e-6 in FP32 is
 // only 31 ulps below 1), while expm1 keeps the decrement to full precision.
+// Lawson (integrating-factor) RK4 stage with the factors given as m1 = expm1(-lin h) and
+// mh = expm1(-lin h / 2)
 template <typename C>
-__device__ __forceinline__ C rk4_combine(int stage, bool expl, C n, C s, C& acc, C vs, decltype(C::x) h,
-                                         decltype(C::x) lin) {
+__device__ __forceinline__ C lawson_combine(int stage, C n, C s, C& acc, decltype(C::x) h, decltype(C::x) m1,
+                                            decltype(C::x) mh) {
   using Re = decltype(C::x);
-  if (expl) {  // classical RK4 with explicit viscosity: k = N - nu k^2 v_stage
-    const C k = mk<C>(n.x - lin * vs.x, n.y - lin * vs.y);
-    if (stage == 1) { acc = k; return mk<C>(s.x + Re(0.5) * h * k.x, s.y + Re(0.5) * h * k.y); }
-    if (stage == 2) { acc = mk<C>(acc.x + Re(2) * k.x, acc.y + Re(2) * k.y);
-                      return mk<C>(s.x + Re(0.5) * h * k.x, s.y + Re(0.5) * h * k.y); }
-    if (stage == 3) { acc = mk<C>(acc.x + Re(2) * k.x, acc.y + Re(2) * k.y);
-                      return mk<C>(s.x + h * k.x, s.y + h * k.y); }
-    const Re h6 = h / Re(6);
-    return mk<C>(s.x + h6 * (acc.x + k.x), s.y + h6 * (acc.y + k.y));
-  }
-  // Lawson (integrating-factor) RK4
-  const Re m1 = rexpm1<Re>(-lin * h), mh = rexpm1<Re>(Re(-0.5) * lin * h);
   const Re e1 = Re(1) + m1, eh = Re(1) + mh;
   if (stage == 1) {  // acc = E1 n;  v = E(h/2)(s + h/2 n)
     acc = mk<C>(e1 * n.x, e1 * n.y);
@@ -126,6 +116,23 @@ __device__ __forceinline__ C rk4_combine(int stage, bool expl, C n, C s, C& acc,
   }
   const Re h6 = h / Re(6);  // s' = E(h) s + h/6 (acc + n)
   return mk<C>(s.x + (m1 * s.x + h6 * (acc.x + n.x)), s.y + (m1 * s.y + h6 * (acc.y + n.y)));
+}
+
+template <typename C>
+__device__ __forceinline__ C rk4_combine(int stage, bool expl, C n, C s, C& acc, C vs, decltype(C::x) h,
+                                         decltype(C::x) lin) {
+  using Re = decltype(C::x);
+  if (expl) {  // classical RK4 with explicit viscosity: k = N - nu k^2 v_stage
+    const C k = mk<C>(n.x - lin * vs.x, n.y - lin * vs.y);
+    if (stage == 1) { acc = k; return mk<C>(s.x + Re(0.5) * h * k.x, s.y + Re(0.5) * h * k.y); }
+    if (stage == 2) { acc = mk<C>(acc.x + Re(2) * k.x, acc.y + Re(2) * k.y);
+                      return mk<C>(s.x + Re(0.5) * h * k.x, s.y + Re(0.5) * h * k.y); }
+    if (stage == 3) { acc = mk<C>(acc.x + Re(2) * k.x, acc.y + Re(2) * k.y);
+                      return mk<C>(s.x + h * k.x, s.y + h * k.y); }
+    const Re h6 = h / Re(6);
+    return mk<C>(s.x + h6 * (acc.x + k.x), s.y + h6 * (acc.y + k.y));
+  }
+  return lawson_combine<C>(stage, n, s, acc, h, rexpm1<Re>(-lin * h), rexpm1<Re>(Re(-0.5) * lin * h));
 }
 
 template <typename R, int N, int F, int MODE>

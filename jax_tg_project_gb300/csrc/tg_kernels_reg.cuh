@@ -602,8 +602,10 @@ struct KxRegShape {
   static constexpr int MMAX = 2 * (N / 3) + 1;
   // per group: state and accumulator tiles [2][3][M][QW], staged by cp.async
   static constexpr long long stage_elems = 2LL * 3 * MMAX * QW;
+  // + the integrating-factor tables: (expm1(-c kx^2) for c = nu h, nu h / 2) over kx, and
+  // the same of ky^2 + kz^2 for the CTA's columns
   static constexpr long long smem =
-      (long long)sizeof(cplx<R>) * (N + (long long)NG * QW * CS + (long long)NG * stage_elems);
+      (long long)sizeof(cplx<R>) * (N + (long long)NG * QW * CS + (long long)NG * stage_elems + MMAX + NG * QW);
   // adjoint kernels, per group: a ring of four [N][QW] input tiles of the forward transforms,
   // or up to two [3][M][QW] spectral tiles, both staged by cp.async
   static constexpr long long ring_elems = 4LL * N * QW;
@@ -645,6 +647,11 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
   C* xcol = tw + N + (grp * QW + col) * CS;
   // [0] state, [1] accumulator: [3][M][QW] each
   C* stg = tw + N + Sh::NG * QW * CS + grp * Sh::stage_elems;
+  // integrating factors of the Lawson stages: expm1(-c (kx^2 + q)) with c = nu h (or nu h / 2)
+  // and q = ky^2 + kz^2 is expm1(a) + expm1(b) + expm1(a) expm1(b), a = -c kx^2, b = -c q, an
+  // exact identity; the kx terms (M entries) and the (ky, kz) terms of the CTA's columns are
+  // tabulated per CTA, so that no mode evaluates expm1 (the factors stay in delta form)
+  C* ftab = tw + N + Sh::NG * QW * CS + Sh::NG * Sh::stage_elems;
   if constexpr (MODE == KX_STAGE) {
     // stage the state (and accumulator) tiles of this group while the forward
     // transforms run: rows of QW consecutive kz are 32-byte aligned (Hz % 4 == 0, kz0 a
@@ -665,8 +672,23 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
     cp_async_commit();
   }
   build_twiddles<Plan>(tw, a.tw, threadIdx.x, Sh::NT);
-  __syncthreads();
   const float kyf = float(ksigned(iyc, K)), kzf = float(kz);
+  if constexpr (MODE == KX_STAGE) {
+    const RunCoef cf0 = a.coef[run];
+    const R c1 = R(cf0.nu * cf0.dt), ch = R(0.5) * c1;
+    for (int i = threadIdx.x; i < M + Sh::NG * QW; i += Sh::NT) {
+      R k2;
+      if (i < M) {
+        const R kx = R(ksigned(i, K));
+        k2 = kx * kx;
+      } else {
+        const R kc = R(blockIdx.y * Sh::NG * QW + (i - M));  // kz of column i - M
+        k2 = R(kyf * kyf) + kc * kc;
+      }
+      ftab[i] = mk<C>(rexpm1<R>(-c1 * k2), rexpm1<R>(-ch * k2));
+    }
+  }
+  __syncthreads();
   const long long soff = (long long)run * 3 * g.sS + (long long)iyc * Hz + kz;  // + (f*M + ic)*M*Hz
 
   C v[3][E];
@@ -721,6 +743,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
     const RunCoef cf = a.coef[run];
     const bool expl = (a.flags & FLAG_EXPLICIT) != 0;
     const R h = R(cf.dt);
+    const C fyz = ftab[M + grp * QW + col];  // the (ky, kz) terms of this column
 #pragma unroll
     for (int q = 0; q < E; ++q) {
       const int ic = kcompact_slot<N, P>(t, q, K);
@@ -728,7 +751,9 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
         const float kx = float(ksigned(ic, K));
         const float k2 = kx * kx + kyf * kyf + kzf * kzf;
         leray(v[0][q], v[1][q], v[2][q], kx, kyf, kzf, k2);
-        const R lin = R(cf.nu * double(k2));
+        const R lin = expl ? R(cf.nu * double(k2)) : R(0);  // explicit viscosity only
+        const C fx = ftab[ic];
+        const R m1 = fmaf(fx.x, fyz.x, fx.x + fyz.x), mh = fmaf(fx.y, fyz.y, fx.y + fyz.y);
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
           const long long o = soff + ((long long)f * M + ic) * M * Hz;
@@ -739,7 +764,8 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
           }
           C acc = (a.stage > 1) ? stg[((long long)(3 + f) * M + ic) * QW + col] : czero<C>();
           const C vs = (expl && a.stage > 1) ? a.vs[o] : s;
-          const C nv = rk4_combine<C>(a.stage, expl, v[f][q], s, acc, vs, h, lin);
+          const C nv = expl ? rk4_combine<C>(a.stage, true, v[f][q], s, acc, vs, h, lin)
+                            : lawson_combine<C>(a.stage, v[f][q], s, acc, h, m1, mh);
           if (a.stage < 4) {
             a.acc[o] = acc;
             if (expl) a.vs[o] = nv;
