@@ -86,6 +86,9 @@ __device__ __forceinline__ void leray(C& a, C& b, C& c, float kx, float ky, floa
 template <typename R> __device__ __forceinline__ R rexpm1(R x);
 template <> __device__ __forceinline__ float rexpm1<float>(float x) { return expm1f(x); }
 template <> __device__ __forceinline__ double rexpm1<double>(double x) { return expm1(x); }
+// expm1(a + b) from x = expm1(a) and y = expm1(b): x + y + x y, an exact identity (the terms
+// share a sign, so the two roundings stay within a few ulps of the result)
+template <typename R> __device__ __forceinline__ R expm1_add(R x, R y) { return fma(x, y, x + y); }
 
 // One RK4 stage for one component: n is the (projected) nonlinear tendency,
 // s the state at the start of the step, lin = nu k^2, h the step.  Returns the

@@ -753,7 +753,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
         leray(v[0][q], v[1][q], v[2][q], kx, kyf, kzf, k2);
         const R lin = expl ? R(cf.nu * double(k2)) : R(0);  // explicit viscosity only
         const C fx = ftab[ic];
-        const R m1 = fmaf(fx.x, fyz.x, fx.x + fyz.x), mh = fmaf(fx.y, fyz.y, fx.y + fyz.y);
+        const R m1 = expm1_add(fx.x, fyz.x), mh = expm1_add(fx.y, fyz.y);
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
           const long long o = soff + ((long long)f * M + ic) * M * Hz;
