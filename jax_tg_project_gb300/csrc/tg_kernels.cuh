@@ -237,20 +237,32 @@ kx_kernel(const PassArgs<R> a) {
       } else {  // KX_STAGE
         const bool expl = (a.flags & FLAG_EXPLICIT) != 0;
         const R h = R(cf.dt);
+        // the state, accumulator (and stage-state) arrays are distinct, and all loads of the
+        // mode are issued before its arithmetic and stores
+        C* __restrict__ Sp = a.S;
+        C* __restrict__ Ap = a.acc;
+        C* __restrict__ Vp = a.vs;
+        C sv[F], av[F];
+#pragma unroll
+        for (int f = 0; f < F; ++f) {
+          const long long o = soff + f * g.sS + m0;
+          sv[f] = Sp[o];
+          av[f] = (a.stage > 1) ? Ap[o] : czero<C>();
+        }
 #pragma unroll
         for (int f = 0; f < F; ++f) {
           const double visc = (f < 3) ? cf.nu : cf.eta;
           const R lin = R(visc * double(k2));
           const long long o = soff + f * g.sS + m0;
-          const C s = a.S[o];
-          C acc = (a.stage > 1 && !(expl && a.stage == 1)) ? a.acc[o] : czero<C>();
-          const C vs = (expl && a.stage > 1) ? a.vs[o] : s;
+          const C s = sv[f];
+          C acc = av[f];
+          const C vs = (expl && a.stage > 1) ? Vp[o] : s;
           const C v = rk4_combine<C>(a.stage, expl, n[f], s, acc, vs, h, lin);
           if (a.stage < 4) {
-            a.acc[o] = acc;
-            if (expl) a.vs[o] = v;
+            Ap[o] = acc;
+            if (expl) Vp[o] = v;
           } else {
-            a.S[o] = v;
+            Sp[o] = v;
           }
           sb[(f * M + ic) * TZ + c] = v;
         }
