@@ -378,11 +378,15 @@ def run_reference(args, rank, world):
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
         "steps": len(times), "warmup": len(warm), "ms_per_step": 1e3 * sum(times) / len(times),
+        # a full 256^3 step takes seconds on the host: the requested counts are capped by the
+        # time budget (--cpu-budget) so that the run ends within minutes
+        "steps_requested": args.steps, "warmup_requested": args.warmup,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": workload_config(n, world),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{len(times)} RK4 step(s) at {n}^3 of the reference JAX "
-                                   "algorithm restated in NumPy/SciPy FP64 (jax is not installed); "
+                                   "algorithm restated in NumPy/SciPy FP64 (jax is not installed; "
+                                   f"{args.steps} requested, capped at {budget:.0f} s of host time); "
                                    f"FFTs on {cores} threads"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
