@@ -145,9 +145,9 @@ int tg_step(tg_plan* plan, void* state, double dt, double nu, double eta, int ns
 int tg_run(tg_plan* plan, void* state, double dt, double nu, double eta, int nsteps,
            int save_every, double* series);
 
-/* One diagnostics record per run into out (device, [batch][TG_DIAG_WIDTH]) with
- * compensated FP64 reductions; the divergence maxima come from a physical-space
- * transform.  Replaces kinetic_energy / enstrophy / viscous_dissipation /
+/* One diagnostics record per run into out (device, [batch][TG_DIAG_WIDTH]): per-mode
+ * terms in the state's precision, deterministic FP64 sums; the divergence maxima come
+ * from a physical-space transform.  Replaces kinetic_energy / enstrophy / viscous_dissipation /
  * spectral_divergence (jax/taylor_green_jax.py:90-128,199-201) and
  * MhdDiagnostics.record (cuda/taylor_green_mhd/diagnostics.py:20-49). */
 int tg_diagnostics(tg_plan* plan, const void* state, double nu, double eta, double* out);
