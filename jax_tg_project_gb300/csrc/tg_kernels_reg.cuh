@@ -610,8 +610,9 @@ struct KxRegShape {
   // or up to two [3][M][QW] spectral tiles, both staged by cp.async
   static constexpr long long ring_elems = 4LL * N * QW;
   static constexpr long long adj_area = (ring_elems > stage_elems) ? ring_elems : stage_elems;
+  // + the integrating-factor tables of the x stage (the tape forms)
   static constexpr long long smem_adj =
-      (long long)sizeof(cplx<R>) * (N + (long long)NG * QW * CS + (long long)NG * adj_area);
+      (long long)sizeof(cplx<R>) * (N + (long long)NG * QW * CS + (long long)NG * adj_area + MMAX + NG * QW);
 };
 
 
@@ -932,8 +933,26 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
     }
   }
   build_twiddles<Plan>(tw, a.tw, threadIdx.x, Sh::NT);
-  __syncthreads();
   const float kyf = float(ksigned(iyc, K)), kzf = float(kz);
+  // the integrating factors exactly as the forward x stage forms them (its per-CTA tables of
+  // expm1 over kx^2 and over ky^2 + kz^2 of the columns, combined by expm1_add)
+  C* ftab = tw + N + Sh::NG * QW * CS + Sh::NG * Sh::adj_area;
+  if constexpr (TAPE) {
+    const RunCoef cf0 = a.coef[run];
+    const R c1 = R(cf0.nu * cf0.dt), ch = R(0.5) * c1;
+    for (int i = threadIdx.x; i < M + Sh::NG * QW; i += Sh::NT) {
+      R k2;
+      if (i < M) {
+        const R kx = R(ksigned(i, K));
+        k2 = kx * kx;
+      } else {
+        const R kc = R(blockIdx.y * Sh::NG * QW + (i - M));
+        k2 = R(kyf * kyf) + kc * kc;
+      }
+      ftab[i] = mk<C>(rexpm1<R>(-c1 * k2), rexpm1<R>(-ch * k2));
+    }
+  }
+  __syncthreads();
   const long long soff = soff0 + col;
   const RunCoef cf = a.coef[run];
   const R h = R(cf.dt);
@@ -951,12 +970,13 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
   using Inv = std::integral_constant<int, +1>;
   const R inv_n3 = R(1) / (R(N) * R(N) * R(N));
   // k^2 and the Lawson factors expm1(-nu k^2 h), expm1(-nu k^2 h / 2) of mode (ic, iyc, kz)
+  // (tape forms: from the tables above)
   auto factors = [&](int ic, R& kk, R& m1, R& mh) {
     const float kx = float(ksigned(ic, K));
     kk = R(kx * kx + kyf * kyf + kzf * kzf);
-    const R lin = R(cf.nu * double(kk));
-    m1 = rexpm1<R>(-lin * h);
-    mh = rexpm1<R>(R(-0.5) * lin * h);
+    const C fx = ftab[ic], fyz = ftab[M + grp * QW + col];
+    m1 = expm1_add(fx.x, fyz.x);
+    mh = expm1_add(fx.y, fyz.y);
   };
   // adjoint seeds of the stage nonlinear terms: mu_s = cl L + cg g_{s+1}
   auto seeds = [&](int s, R e1, R eh, R& cl, R& cg) {
