@@ -179,7 +179,8 @@ class Plan:
 
     def run(self, state, dt=-1.0, nu=-1.0, eta=-1.0, nsteps=1, save_every=1):
         self._check_state(state)
-        nrec = 1 + nsteps // save_every + (1 if nsteps % save_every else 0)
+        # (save_every < 1 is rejected by tg_run with TG_E_INVALID)
+        nrec = 1 + (nsteps // save_every + (1 if nsteps % save_every else 0) if save_every >= 1 else 0)
         series = torch.zeros((nrec, self.batch, _abi.TG_DIAG_WIDTH), dtype=torch.float64,
                              device=self.device)
         self._sync_stream()
