@@ -49,6 +49,11 @@ template <> struct PlanFor<512> { using T = FftPlan<512, 64, 8, 8, 8>; };  // 64
 // column would make them 1024 threads wide (measured 1.15 ms against 0.78 ms at 512^3)
 template <int N> struct YPlanFor { using T = typename PlanFor<N>::T; };
 template <> struct YPlanFor<512> { using T = FftPlan<512, 16, 16, 32>; };
+// the shared-memory x pass at 128 (the MHD stage, FP64 plans): 16 threads a column (E = 8),
+// two 256-thread CTAs per SM in FP32.  Its grid is 85 x 3 CTAs at 128^3, so 8 threads a
+// column left 7 warps per SM
+template <int N> struct XPlanFor { using T = typename PlanFor<N>::T; static constexpr int MINB = 1; };
+template <> struct XPlanFor<128> { using T = FftPlan<128, 16, 8, 2, 8>; static constexpr int MINB = 2; };
 
 __host__ __device__ constexpr int kept_of(int n) { return n / 3; }
 

@@ -139,10 +139,10 @@ __device__ __forceinline__ C rk4_combine(int stage, bool expl, C n, C s, C& acc,
 }
 
 template <typename R, int N, int F, int MODE>
-__global__ void __launch_bounds__(PlanFor<N>::T::P * TileZ<R, N, F>::value)
+__global__ void __launch_bounds__(XPlanFor<N>::T::P * TileZ<R, N, F>::value, (sizeof(R) == 4) ? XPlanFor<N>::MINB : 1)
 kx_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
-  using Plan = typename PlanFor<N>::T;
+  using Plan = typename XPlanFor<N>::T;
   constexpr int P = Plan::P, TZ = TileZ<R, N, F>::value, CS = ColLayout<N>::CS, NT = P * TZ;
   const Geo g = a.g;
   const int K = g.K, M = g.M, Hz = g.Hz;
@@ -627,7 +627,7 @@ static cudaError_t set_smem(K kernel, long long bytes) {
 template <typename R, int N, int F, int MODE>
 static cudaError_t launch_kx(const PassArgs<R>& a, int runs, cudaStream_t st) {
   constexpr int TZ = TileZ<R, N, F>::value;
-  constexpr int NT = PlanFor<N>::T::P * TZ;
+  constexpr int NT = XPlanFor<N>::T::P * TZ;
   const long long smem = TileZ<R, N, F>::smem(TZ);
   static cudaError_t attr = set_smem(kx_kernel<R, N, F, MODE>, smem);
   if (attr != cudaSuccess) return attr;
