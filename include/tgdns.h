@@ -93,6 +93,8 @@ typedef struct tg_desc {
   int cutoff;    /* kept |k| per axis; <= 0 selects the reference 2/3 rule */
 } tg_desc;
 
+/* One device per process: kernels' shared-memory attributes are set once per process, on
+ * the device current at their first launch; drive several GPUs as one process each. */
 /* Create / destroy a plan (scratch buffers, twiddle tables, CUDA graphs).
  * Replaces the set-up of SpectralGrid (cuda/taylor_green_cuda/grid.py:5-13),
  * make_wavenumbers / make_dealias_mask (jax/taylor_green_jax.py:55-67) and the
