@@ -206,3 +206,32 @@ def test_splitmix64_known_answers():
     # outputs are splitmix64(k * golden_gamma) for k = 0, 1, 2
     out = perturb.splitmix64(np.array([0, 0x9E3779B97F4A7C15, 0x3C6EF372FE94F82A], dtype=np.uint64))
     assert [int(x) for x in out] == [0xE220A8397B1DCDAF, 0x6E789E6AA1B965F4, 0x06C45D188009454F]
+
+
+def _band_limited(N, seed):
+    """A real, solenoidal, dealiased random field: the compact layout holds it exactly."""
+    rng = np.random.default_rng(seed)
+    kx, ky, kz = T.make_wavenumbers(N)
+    mask = T.make_dealias_mask(N)
+    uh = np.fft.fftn(rng.standard_normal((3, N, N, N)), axes=(-3, -2, -1)) * mask
+    k2 = kx * kx + ky * ky + kz * kz
+    k2[0, 0, 0] = 1.0
+    div = (kx * uh[0] + ky * uh[1] + kz * uh[2]) / k2
+    uh = uh - np.stack([kx, ky, kz]) * div
+    return np.real(np.fft.ifftn(uh, axes=(-3, -2, -1))), kx, ky, kz
+
+
+@pytest.mark.parametrize("N", [12, 16, 24])
+def test_compact_layout_round_trip_and_parseval(N):
+    """The oracle's compact half-spectrum helpers (the reference layout of the GPU state tests):
+    physical -> compact -> physical is the identity on dealiased real fields, and Parseval on the
+    compact coefficients equals the reference's physical-space diagnostics."""
+    u, kx, ky, kz = _band_limited(N, seed=N)
+    c = T.compact_from_physical(u)
+    K = N // 3
+    assert c.shape == (3, 2 * K + 1, 2 * K + 1, K + 1)
+    np.testing.assert_allclose(T.physical_from_compact(c, N), u, rtol=0, atol=1e-12)
+    ke, ens, diss = T.compact_diagnostics(c, nu=0.01)[:3]
+    assert ke == pytest.approx(T.kinetic_energy(u), rel=1e-12)
+    assert ens == pytest.approx(T.enstrophy(u, kx, ky, kz), rel=1e-12)
+    assert diss == pytest.approx(T.viscous_dissipation(u, 0.01, kx, ky, kz), rel=1e-12)
