@@ -48,3 +48,21 @@ def test_errors_are_reported_without_a_gpu():
     desc = _abi.TgDesc(64, 0, 0, 0, 0, 0)
     assert lib.tg_plan_create(ctypes.byref(h), ctypes.byref(desc)) == _abi.TG_E_INVALID
     assert lib.tg_step(None, None, 0.1, 0.01, 0.0, 1) == _abi.TG_E_INVALID
+
+
+def declared_arity():
+    """Parameter count of every tg_* declaration in the header (comments removed)."""
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(tg_\w+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_ctypes_signatures_match_the_header_arity():
+    from jax_tg_project_gb300 import _abi
+    arity = declared_arity()
+    assert set(arity) == set(_abi.SIGNATURES)
+    for name, (_, argtypes) in _abi.SIGNATURES.items():
+        assert len(argtypes) == arity[name], (name, len(argtypes), arity[name])
