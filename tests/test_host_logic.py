@@ -103,3 +103,22 @@ def test_cli_parser_accepts_the_reference_flags():
     with pytest.raises(SystemExit) as e:
         cli.main(["hydro", "--no-such-flag"])
     assert e.value.code != 0
+
+
+def test_product_modules_never_import_the_oracle():
+    """The oracle is test infrastructure: importing every module of the package (in a fresh
+    interpreter) must not load it."""
+    import subprocess
+    import sys
+    mods = ["jax_tg_project_gb300", "jax_tg_project_gb300.plan", "jax_tg_project_gb300.taylor_green",
+            "jax_tg_project_gb300.spectral", "jax_tg_project_gb300.mhd", "jax_tg_project_gb300.config",
+            "jax_tg_project_gb300.ensemble", "jax_tg_project_gb300.adjoint", "jax_tg_project_gb300.cli",
+            "jax_tg_project_gb300.plots", "jax_tg_project_gb300._abi", "jax_tg_project_gb300._runtime"]
+    code = ("import importlib, sys\n"
+            f"for m in {mods!r}: importlib.import_module(m)\n"
+            "bad = [m for m in sys.modules if m == 'oracle' or m.startswith('oracle.')]\n"
+            "assert not bad, bad\n")
+    import os
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
