@@ -57,7 +57,11 @@ enum {
                                 instead of the physical +(j x b) */
   TG_FLAG_AUTOTUNE = 4       /* tg_plan_create times the pass variants (register-resident
                                 or shared-memory x and z passes) on this plan's shape and
-                                keeps the fastest (tg_pass_variant); no reference counterpart */
+                                batch, then the y-pass configurations (radix plan and kz
+                                columns per CTA), and keeps the fastest (tg_pass_variant,
+                                tg_y_config).  TG_PASS_VARIANT / TG_Y_CONF in the environment
+                                force a choice; with TG_AUTOTUNE_CACHE naming a file, choices
+                                are read from and appended to it.  No reference counterpart */
 };
 enum {
   TG_IC_TAYLOR_GREEN = 0,     /* u = (sin x cos y cos z, -cos x sin y cos z, 0); b = 0 */
@@ -195,6 +199,12 @@ int tg_profile_passes(tg_plan* plan, void* state, double dt, double nu, double e
  * else 0 (or the TG_PASS_VARIANT environment variable).  No reference counterpart. */
 int tg_pass_variant(const tg_plan* plan);
 
+/* y-pass configuration in use (0 = the default radix plan and tile width); *count (if not
+ * null) receives the number of configurations built for this size and precision.  Chosen by
+ * TG_FLAG_AUTOTUNE, else 0 (or the TG_Y_CONF environment variable).  No reference
+ * counterpart. */
+int tg_y_config(const tg_plan* plan, int* count);
+
 /* Kernels launched by the last tg_step / tg_run call (for launch accounting). */
 int64_t tg_last_launch_count(const tg_plan* plan);
 
@@ -235,15 +245,18 @@ int tg_energy_spectrum(tg_plan* plan, const void* state, double* out);
  * E_m, H_c, E_k+E_m) of a state laid out as a plan with the default 2/3 cutoff
  * would lay it out (n, batch, physics, precision as in tg_desc) into out
  * ([batch][TG_DIAG_WIDTH] doubles, device); slots 6-7 (divergence maxima) are
- * not computed and are set to -1.  Its only scratch is a file-scope device
- * array of TG_NOALLOC_MAX_RUNS*96*5 doubles (240 KiB) that every GPU loading the
- * library holds until the process exits; batch > TG_NOALLOC_MAX_RUNS is rejected
- * with TG_E_INVALID.  The first call on each device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current: make that first call
- * before any stream capture.  All calls share the array: calls that overlap on
- * the GPU race and must be ordered by the caller.  Calls no cudaMalloc/cudaFree
- * and no allocating library routine.  eta is unused (kept for symmetry with
- * tg_diagnostics).  Asynchronous on stream. */
+ * not computed and are set to -1.  n must be a size tg_plan_create builds for the
+ * precision (else TG_E_UNSUPPORTED); nu >= 0 is used as given (there is no plan
+ * whose nu a negative value could select: TG_E_INVALID).  Its only scratch is a
+ * file-scope device array of TG_NOALLOC_MAX_RUNS*96*5 doubles (240 KiB) that every
+ * GPU loading the library holds until the process exits; batch >
+ * TG_NOALLOC_MAX_RUNS is rejected with TG_E_INVALID.  The first call on each device
+ * (more exactly: in each CUDA context, so again after a device reset) looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current: make that
+ * first call before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race and must be ordered by the caller.  Calls no
+ * cudaMalloc/cudaFree and no allocating library routine.  eta is unused (kept for
+ * symmetry with tg_diagnostics).  Asynchronous on stream. */
 #define TG_NOALLOC_MAX_RUNS 64
 int tg_diagnostics_noalloc(const void* state, int n, int batch, int physics, int precision, double nu,
                            double eta, double* out, void* stream);

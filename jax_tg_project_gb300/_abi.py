@@ -68,6 +68,7 @@ SIGNATURES = {
                                        c_void_p, c_void_p]),
     "tg_last_launch_count": (c_int64, [c_void_p]),
     "tg_pass_variant": (c_int, [c_void_p]),
+    "tg_y_config": (c_int, [c_void_p, ctypes.POINTER(c_int)]),
     "tg_release_host_tape": (c_int, [c_void_p]),
     "tg_last_error": (ctypes.c_char_p, []),
     "tg_version": (c_int, []),

@@ -22,7 +22,8 @@ namespace tg {
   X(float, 64) X(float, 96) X(float, 128) X(float, 256) X(float, 512)
 #define TG_SIZES_F64(X) X(double, 8) X(double, 16) X(double, 32) X(double, 64) X(double, 96) \
   X(double, 128) X(double, 256)
-#define TG_DECL(R, N) cudaError_t launch_##R##_##N(int, const PassArgs<R>&, int, cudaStream_t);
+#define TG_DECL(R, N) cudaError_t launch_##R##_##N(int, const PassArgs<R>&, int, cudaStream_t); \
+  int yconfs_##R##_##N();
 TG_SIZES_F32(TG_DECL)
 TG_SIZES_F64(TG_DECL)
 #undef TG_DECL
@@ -52,6 +53,18 @@ static LaunchFn<double> find_f64(int n) {
     TG_SIZES_F64(TG_CASE)
 #undef TG_CASE
     default: return nullptr;
+  }
+}
+// y-pass configurations built for a size (1 where the autotuner has no alternatives)
+static int yconf_count(int n, int prec) {
+  switch (prec == TG_PREC_F64 ? -n : n) {
+#define TG_CASE(R, N) case N: return yconfs_##R##_##N();
+    TG_SIZES_F32(TG_CASE)
+#undef TG_CASE
+#define TG_CASE(R, N) case -N: return yconfs_##R##_##N();
+    TG_SIZES_F64(TG_CASE)
+#undef TG_CASE
+    default: return 1;
   }
 }
 
@@ -605,6 +618,10 @@ static thread_local std::string g_last_error;
 namespace tg {
 // lets other translation units of the library report through tg_last_error()
 void set_last_error(const std::string& message) { g_last_error = message; }
+// whether the pass kernels of an n^3 grid are built for a precision (TG_PREC_*)
+bool size_built(int n, int prec) {
+  return prec == TG_PREC_F64 ? (find_f64(n) != nullptr) : (find_f32(n) != nullptr);
+}
 }  // namespace tg
 
 static int fail(int code, const std::string& msg) {
@@ -652,6 +669,8 @@ struct tg_plan {
   int64_t launches = 0;
   int64_t scratch = 0;
   int variant = 0;  // pass variant: bit 0 shared-memory z passes, bit 1 shared-memory x passes
+  int yconf = 0;    // y-pass configuration (radix plan, kz columns per CTA), 0 = default
+  int nyconf = 1;   // configurations built for this size and precision
   // per-launch CUDA events (op, start, stop) while tg_profile_passes runs
   std::vector<ProfEvent>* prof = nullptr;
 };
@@ -676,6 +695,7 @@ struct Ops {
     a.coef = p->coef;
     a.amax = p->amax;
     a.variant = p->variant;
+    a.yconf = p->yconf;
     if (p->flags & TG_FLAG_EXPLICIT_VISC) a.flags |= FLAG_EXPLICIT;
     return a;
   }
@@ -956,9 +976,7 @@ int advance(tg_plan* p, void* S, int nsteps) {
   return TG_OK;
 }
 
-bool size_supported(int n, int prec) {
-  return prec == TG_PREC_F64 ? (find_f64(n) != nullptr) : (find_f32(n) != nullptr);
-}
+bool size_supported(int n, int prec) { return tg::size_built(n, prec); }
 
 }  // namespace
 
@@ -968,52 +986,144 @@ extern "C" {
 const char* tg_last_error(void) { return g_last_error.c_str(); }
 int tg_version(void) { return 100; }
 
-// TG_FLAG_AUTOTUNE: time the distinct pass variants (register-resident or shared-memory
-// x and z passes) on this plan's shape -- graph-launched steps of a perturbed
-// Taylor-Green state -- and keep the fastest
+// ---------------------------------------------------------------- autotuning
+// TG_FLAG_AUTOTUNE times, on this plan's own shape and batch (graph-launched steps of a
+// perturbed Taylor-Green state), first the pass variants (register-resident or
+// shared-memory x and z passes), then with the fastest variant the y-pass configurations
+// (radix plan and kz columns per CTA, YConf in tg_common.cuh), and keeps the fastest of
+// each.  TG_PASS_VARIANT / TG_Y_CONF force a choice and skip its timing.  With
+// TG_AUTOTUNE_CACHE naming a file, choices are looked up there first (keyed by device,
+// grid size, batch, physics, precision, cutoff and scheme) and new ones are appended.
+
+// best of two timings of three graph-launched steps (after the eager step and capture)
+static int time_steps(tg_plan* p, void* S, cudaEvent_t e0, cudaEvent_t e1, float* best) {
+  drop_graph(p);
+  int rc;
+  if ((rc = tg_step(p, S, 1e-4, 1e-2, 1e-2, 2))) return rc;  // eager step, capture, one replay
+  *best = 1e30f;
+  for (int rep = 0; rep < 2; ++rep) {
+    cudaEventRecord(e0, p->st);
+    if ((rc = tg_step(p, S, 1e-4, 1e-2, 1e-2, 3))) return rc;
+    cudaEventRecord(e1, p->st);
+    float ms = 0.0f;
+    cudaError_t e;
+    if ((e = cudaEventSynchronize(e1)) != cudaSuccess || (e = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess)
+      return cuda_fail(e, "autotune timing");
+    *best = std::min(*best, ms);
+  }
+  return TG_OK;
+}
+
+static std::string tune_key(const tg_plan* p) {
+  int dev = 0;
+  cudaDeviceProp prop;
+  std::string name = "unknown";
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaGetDeviceProperties(&prop, dev) == cudaSuccess) {
+    name = prop.name;
+    name += "_sm" + std::to_string(prop.major) + std::to_string(prop.minor);
+  }
+  for (char& c : name)
+    if (c == ' ' || c == '\t') c = '_';
+  const int scheme = p->flags & (TG_FLAG_EXPLICIT_VISC | TG_FLAG_LORENTZ_REF);
+  return "tg-autotune-v1 " + name + " n=" + std::to_string(p->n) + " batch=" + std::to_string(p->batch) +
+         " F=" + std::to_string(p->F) + " prec=" + std::to_string(p->prec) + " K=" + std::to_string(p->K) +
+         " scheme=" + std::to_string(scheme);
+}
+
+// the cached (variant, yconf) of this plan's key, if any (the last matching line wins)
+static bool cache_lookup(const char* path, const std::string& key, int* variant, int* yconf) {
+  FILE* f = std::fopen(path, "r");
+  if (!f) return false;
+  char line[512];
+  bool found = false;
+  while (std::fgets(line, sizeof(line), f)) {
+    std::string l(line);
+    const size_t at = l.find(" variant=");
+    if (at == std::string::npos || l.compare(0, at, key) != 0 || at != key.size()) continue;
+    int v = -1, y = -1;
+    if (std::sscanf(l.c_str() + at, " variant=%d yconf=%d", &v, &y) == 2) {
+      *variant = v;
+      *yconf = y;
+      found = true;
+    }
+  }
+  std::fclose(f);
+  return found;
+}
+
+static void cache_store(const char* path, const std::string& key, int variant, int yconf) {
+  FILE* f = std::fopen(path, "a");  // one short line per append
+  if (!f) return;                   // a cache that cannot be written only costs a re-tune
+  std::fprintf(f, "%s variant=%d yconf=%d\n", key.c_str(), variant, yconf);
+  std::fclose(f);
+}
+
 static int autotune(tg_plan* p) {
   const bool f32 = p->prec == TG_PREC_F32;
-  const bool reg_z = f32 && has_reg_adjoint(p->n);                             // z: 16 ... 256
+  const bool reg_z = f32 && (has_reg_adjoint(p->n) || (p->F == 3 && p->n == 96));  // z: 16 ... 256, hydro 96
   const bool reg_x = f32 && p->F == 3 && (has_reg_adjoint(p->n) || p->n == 96);  // x: hydro
+  const bool tune_variant = !std::getenv("TG_PASS_VARIANT");
+  const bool tune_y = !std::getenv("TG_Y_CONF") && p->nyconf > 1;
   std::vector<int> cands = {0};
-  if (reg_z) cands.push_back(1);
-  if (reg_x) cands.push_back(2);
-  if (reg_z && reg_x) cands.push_back(3);
-  if (cands.size() == 1) return TG_OK;
+  if (tune_variant) {
+    if (reg_z) cands.push_back(1);
+    if (reg_x) cands.push_back(2);
+    if (reg_z && reg_x) cands.push_back(3);
+  }
+  if (cands.size() == 1 && !tune_y) return TG_OK;
+  const char* cache = std::getenv("TG_AUTOTUNE_CACHE");
+  const std::string key = cache ? tune_key(p) : std::string();
+  if (cache) {
+    int v = -1, y = -1;
+    if (cache_lookup(cache, key, &v, &y) && v >= 0 && v <= 3 && y >= 0 && y < p->nyconf) {
+      if (tune_variant) p->variant = v;
+      if (tune_y) p->yconf = y;
+      return TG_OK;
+    }
+  }
   void* S = nullptr;
   const size_t bytes = csize(p) * (size_t)p->batch * p->F * p->g.sS;
   cudaError_t e = cudaMalloc(&S, bytes);
   if (e != cudaSuccess) return cuda_fail(e, "autotune state");
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  int rc = TG_OK, best = 0;
-  float best_ms = 1e30f;
+  int rc = TG_OK;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) rc = TG_E_CUDA;
   if (!rc) rc = tg_initial_condition(p, p->F == 6 ? TG_IC_MHD_EQUAL_ENERGY : TG_IC_TAYLOR_GREEN, 1, 1e-3, 4.0,
                                      0.0, S);
-  for (int v : cands) {
-    if (rc) break;
-    p->variant = v;
-    drop_graph(p);
-    if ((rc = tg_step(p, S, 1e-4, 1e-2, 1e-2, 2))) break;  // eager step, capture, one replay
-    cudaEventRecord(e0, p->st);
-    if ((rc = tg_step(p, S, 1e-4, 1e-2, 1e-2, 3))) break;
-    cudaEventRecord(e1, p->st);
-    float ms = 0.0f;
-    if ((e = cudaEventSynchronize(e1)) != cudaSuccess || (e = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess) {
-      rc = cuda_fail(e, "autotune timing");
-      break;
+  if (!rc && cands.size() > 1) {
+    int best = p->variant;
+    float best_ms = 1e30f;
+    for (int v : cands) {
+      p->variant = v;
+      float ms = 0.0f;
+      if ((rc = time_steps(p, S, e0, e1, &ms))) break;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = v;
+      }
     }
-    if (ms < best_ms) {
-      best_ms = ms;
-      best = v;
-    }
+    p->variant = best;
   }
-  p->variant = best;
+  if (!rc && tune_y) {
+    int best = 0;
+    float best_ms = 1e30f;
+    for (int y = 0; y < p->nyconf; ++y) {
+      p->yconf = y;
+      float ms = 0.0f;
+      if ((rc = time_steps(p, S, e0, e1, &ms))) break;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = y;
+      }
+    }
+    p->yconf = best;
+  }
   drop_graph(p);
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   cudaFree(S);
   p->launches = 0;
+  if (!rc && cache) cache_store(cache, key, p->variant, p->yconf);
   return rc;
 }
 
@@ -1043,6 +1153,8 @@ int tg_plan_create(tg_plan** out, const tg_desc* d) {
   p->F = d->physics == TG_PHYS_MHD ? 6 : 3;
   p->G = 2 * p->F;
   if (const char* v = std::getenv("TG_PASS_VARIANT")) p->variant = std::atoi(v);
+  p->nyconf = yconf_count(d->n, d->precision);
+  if (const char* v = std::getenv("TG_Y_CONF")) p->yconf = std::max(0, std::min(std::atoi(v), p->nyconf - 1));
   Geo& g = p->g;
   g.n = n;
   g.K = K;
@@ -1112,7 +1224,7 @@ int tg_plan_create(tg_plan** out, const tg_desc* d) {
     tg_plan_destroy(p);
     return cuda_fail(e, "tg_plan_create: init");
   }
-  if ((p->flags & TG_FLAG_AUTOTUNE) && !std::getenv("TG_PASS_VARIANT")) {
+  if (p->flags & TG_FLAG_AUTOTUNE) {
     const int rc = autotune(p);
     if (rc) {
       tg_plan_destroy(p);
@@ -1124,6 +1236,11 @@ int tg_plan_create(tg_plan** out, const tg_desc* d) {
 }
 
 int tg_pass_variant(const tg_plan* p) { return p ? p->variant : 0; }
+
+int tg_y_config(const tg_plan* p, int* count) {
+  if (count) *count = p ? p->nyconf : 0;
+  return p ? p->yconf : 0;
+}
 
 int tg_release_host_tape(tg_plan* p) {
   if (!p) return fail(TG_E_INVALID, "tg_release_host_tape: null plan");

@@ -49,6 +49,31 @@ template <> struct PlanFor<512> { using T = FftPlan<512, 64, 8, 8, 8>; };  // 64
 // column would make them 1024 threads wide (measured 1.15 ms against 0.78 ms at 512^3)
 template <int N> struct YPlanFor { using T = typename PlanFor<N>::T; };
 template <> struct YPlanFor<512> { using T = FftPlan<512, 16, 16, 32>; };
+
+// y-pass configurations (radix plan, kz columns per CTA) that plan creation with
+// TG_FLAG_AUTOTUNE times on the plan's own shape; configuration 0 is the default.  The
+// column count sets the width of each CTA's row segments (8 bytes a column) and how many
+// padding columns the last tile of a row carries.
+template <int N> constexpr int ytile_default() { return (N >= 128) ? 16 : ((N >= 12) ? 8 : 4); }
+template <int N, int I> struct YConf { using Plan = typename YPlanFor<N>::T; static constexpr int TZ = ytile_default<N>(); };
+template <int N> struct YConfCount { static constexpr int value = 1; };
+template <> struct YConfCount<32> { static constexpr int value = 4; };
+template <> struct YConf<32, 1> { using Plan = PlanFor<32>::T; static constexpr int TZ = 4; };
+template <> struct YConf<32, 2> { using Plan = PlanFor<32>::T; static constexpr int TZ = 12; };
+template <> struct YConf<32, 3> { using Plan = FftPlan<32, 8, 4, 2, 4>; static constexpr int TZ = 8; };
+template <> struct YConfCount<64> { static constexpr int value = 4; };
+template <> struct YConf<64, 1> { using Plan = PlanFor<64>::T; static constexpr int TZ = 12; };
+template <> struct YConf<64, 2> { using Plan = PlanFor<64>::T; static constexpr int TZ = 16; };
+template <> struct YConf<64, 3> { using Plan = FftPlan<64, 16, 4, 4, 4>; static constexpr int TZ = 8; };
+template <> struct YConfCount<96> { static constexpr int value = 4; };
+template <> struct YConf<96, 1> { using Plan = PlanFor<96>::T; static constexpr int TZ = 12; };
+template <> struct YConf<96, 2> { using Plan = PlanFor<96>::T; static constexpr int TZ = 16; };
+template <> struct YConf<96, 3> { using Plan = FftPlan<96, 4, 8, 12>; static constexpr int TZ = 12; };
+template <> struct YConfCount<128> { static constexpr int value = 3; };
+template <> struct YConf<128, 1> { using Plan = PlanFor<128>::T; static constexpr int TZ = 12; };
+template <> struct YConf<128, 2> { using Plan = FftPlan<128, 16, 8, 2, 8>; static constexpr int TZ = 16; };
+template <> struct YConfCount<256> { static constexpr int value = 2; };
+template <> struct YConf<256, 1> { using Plan = FftPlan<256, 32, 8, 4, 8>; static constexpr int TZ = 8; };
 // the shared-memory x pass at 128 (the MHD stage, FP64 plans): 16 threads a column (E = 8),
 // two 256-thread CTAs per SM in FP32.  Its grid is 85 x 3 CTAs at 128^3, so 8 threads a
 // column left 7 warps per SM
@@ -110,6 +135,7 @@ template <typename R> struct PassArgs {
   int map;               // FieldMap for KX_LOAD
   int nin, nout;         // fields read / written by this pass
   int variant;           // 0: register-resident x/z passes where built, 1: shared-memory passes
+  int yconf;             // y-pass configuration (YConf index, 0 = default)
   cplx<R>* tape;         // KX_STAGE (batch 1): the step tape [V, n1, n2, n3], or null
   const cplx<R>* tp[4];  // FLAG_TAPE adjoint stage kernels: the step tape V, n1, n2, n3
   cplx<R>* out2;         // KX_ADJ_LOAD_T with nout = 9: the three a = P mu fields (x-pass layout)

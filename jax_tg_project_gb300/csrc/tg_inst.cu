@@ -16,13 +16,18 @@
 #define TG_CAT(a, b, c) TG_CAT2(a, b, c)
 
 namespace tg {
+// number of y-pass configurations the autotuner may choose among (FP32 plans)
+int TG_CAT(yconfs, TG_REAL, TG_N)() { return std::is_same<TG_REAL, float>::value ? YConfCount<TG_N>::value : 1; }
+
 cudaError_t TG_CAT(launch, TG_REAL, TG_N)(int op, const PassArgs<TG_REAL>& a, int runs, cudaStream_t st) {
   // a.variant: bit 0 selects the shared-memory z passes, bit 1 the shared-memory x passes
   const bool reg_z = (a.variant & 1) == 0, reg_x = (a.variant & 2) == 0;
   (void)reg_z;
   (void)reg_x;
-  if constexpr (std::is_same<TG_REAL, float>::value && HasRegZ<TG_N>::value) {
+  if constexpr (std::is_same<TG_REAL, float>::value && HasRegZHydro<TG_N>::value) {
     if (reg_z && op == OP_KZ_PROD_HD) return launch_kz_reg<TG_REAL, TG_N>(a, runs, st);
+  }
+  if constexpr (std::is_same<TG_REAL, float>::value && HasRegZ<TG_N>::value) {
     if (reg_z && op == OP_KZ_PROD_MHD) return launch_kz_reg_mhd<TG_REAL, TG_N>(a, runs, st);
     if (reg_z && op == OP_KZ_ADJ) return launch_kz_reg_adj<TG_REAL, TG_N>(a, runs, st);
     const bool tape = (a.flags & FLAG_TAPE) != 0;

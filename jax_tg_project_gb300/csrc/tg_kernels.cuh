@@ -12,6 +12,8 @@
 //              C2R -> u x omega (+ j x b, u x b) -> R2C, or plain C2R / R2C.
 #pragma once
 
+#include <type_traits>
+
 #include "tg_common.cuh"
 
 namespace tg {
@@ -292,12 +294,12 @@ kx_kernel(const PassArgs<R> a) {
 }
 
 // ------------------------------------------------------------------ y pass
-template <typename R, int N, int DIR>
-__global__ void __launch_bounds__(YPlanFor<N>::T::P * TileZ<R, N, 3>::base)
+template <typename R, int N, int DIR, int YC>
+__global__ void __launch_bounds__(YConf<N, YC>::Plan::P * YConf<N, YC>::TZ)
 ky_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
-  using Plan = typename YPlanFor<N>::T;
-  constexpr int P = Plan::P, TZ = TileZ<R, N, 3>::base, CS = ColLayout<N>::CS, NT = P * TZ;
+  using Plan = typename YConf<N, YC>::Plan;
+  constexpr int P = Plan::P, TZ = YConf<N, YC>::TZ, CS = ColLayout<N>::CS, NT = P * TZ;
   const Geo g = a.g;
   const int K = g.K, M = g.M, Hz = g.Hz;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -371,6 +373,10 @@ kz_kernel(const PassArgs<R> a) {
   const long long row0 = ((long long)x * N + y0) * Hz;  // row (x, y0); row (x, y0+1) is + Hz
   build_twiddles<Plan>(tw, a.tw, threadIdx.x, NT);
   __syncthreads();
+  // after the twiddles, a pair's buffers are private to its P threads: when they lie in one
+  // warp (P divides 32) the exchanges and buffer hand-overs need only a warp barrier
+  using ZSync = typename std::conditional<(P <= 32 && 32 % P == 0), WarpSync, CtaSync>::type;
+  const ZSync zsync;
 
   // Hermitian packing of rows (x,y0) and (x,y0+1) of one spectral field: Z = A + iB
   auto packed = [&](const C* fld) {
@@ -417,7 +423,7 @@ kz_kernel(const PassArgs<R> a) {
     for (int c = 0; c < 6; ++c) {
       const int fi = (c < 3) ? c : 3 + c;  // u -> 0..2, a -> 6..8
       auto src = packed(yin + fi * g.sY);
-      fft_column<Plan, +1>(t, src, dst_reg, xcol, tw);
+      fft_column<Plan, +1>(t, src, dst_reg, xcol, tw, zsync);
 #pragma unroll
       for (int e = 0; e < E; ++e) ph[c * CS + padx(pt(e))] = zr[e];
     }
@@ -429,7 +435,7 @@ kz_kernel(const PassArgs<R> a) {
 #pragma unroll
     for (int w = 0; w < 3; ++w) {  // (omega x a)_{w+1} -= omega_w a_{w+2};  (omega x a)_{w+2} += omega_w a_{w+1}
       auto src = packed(yin + (3 + w) * g.sY);
-      fft_column<Plan, +1>(t, src, dst_reg, xcol, tw);
+      fft_column<Plan, +1>(t, src, dst_reg, xcol, tw, zsync);
       const int c1 = (w + 1) % 3, c2 = (w + 2) % 3;
 #pragma unroll
       for (int e = 0; e < E; ++e) {
@@ -453,15 +459,15 @@ kz_kernel(const PassArgs<R> a) {
 #pragma unroll
       for (int c = 0; c < 3; ++c) ph[c * CS + n] = macc(c, e);
     }
-    __syncthreads();
+    zsync();
     for (int c = 0; c < 6; ++c) {
       C* pc = ph + c * CS;
       auto src = [&](int n, int) -> C { return pc[padx(n)]; };
-      fft_column<Plan, -1>(t, src, dst_reg, xcol, tw);
-      __syncthreads();
+      fft_column<Plan, -1>(t, src, dst_reg, xcol, tw, zsync);
+      zsync();
 #pragma unroll
       for (int e = 0; e < E; ++e) pc[padx(pt(e))] = zr[e];
-      __syncthreads();
+      zsync();
       unpack_store(pc, zout + c * g.sY);
     }
   } else if constexpr (MODE == KZ_PROD_HD || MODE == KZ_PROD_MHD) {
@@ -481,7 +487,7 @@ kz_kernel(const PassArgs<R> a) {
     for (int c = 0; c < Sh::NPH; ++c) {
       const int fi = (c < 3) ? c : 3 + c;  // G order: u, omega, b, j
       auto src = packed(yin + fi * g.sY);
-      fft_column<Plan, +1>(t, src, dst_reg, xcol, tw);
+      fft_column<Plan, +1>(t, src, dst_reg, xcol, tw, zsync);
 #pragma unroll
       for (int e = 0; e < E; ++e) ph[c * CS + padx(pt(e))] = zr[e];
     }
@@ -494,7 +500,7 @@ kz_kernel(const PassArgs<R> a) {
 #pragma unroll
     for (int w = 0; w < 3; ++w) {
       auto src = packed(yin + (3 + w) * g.sY);
-      fft_column<Plan, +1>(t, src, dst_reg, xcol, tw);
+      fft_column<Plan, +1>(t, src, dst_reg, xcol, tw, zsync);
       // (u x omega): omega_x -> m_y += u_z w_x, m_z -= u_y w_x; cyclic
       const int c1 = (w + 1) % 3, c2 = (w + 2) % 3;
 #pragma unroll
@@ -514,7 +520,7 @@ kz_kernel(const PassArgs<R> a) {
 #pragma unroll
       for (int w = 0; w < 3; ++w) {  // j (fields 9..11): m += s (j x b)
         auto src = packed(yin + (9 + w) * g.sY);
-        fft_column<Plan, +1>(t, src, dst_reg, xcol, tw);
+        fft_column<Plan, +1>(t, src, dst_reg, xcol, tw, zsync);
         const int c1 = (w + 1) % 3, c2 = (w + 2) % 3;
 #pragma unroll
         for (int e = 0; e < E; ++e) {
@@ -548,16 +554,16 @@ kz_kernel(const PassArgs<R> a) {
         for (int c = 0; c < 3; ++c) ph[c * CS + n] = macc(c, e);
       }
     }
-    __syncthreads();
+    zsync();
     // forward transforms of the products
     for (int c = 0; c < F; ++c) {
       C* pc = ph + c * CS;
       auto src = [&](int n, int) -> C { return pc[padx(n)]; };
-      fft_column<Plan, -1>(t, src, dst_reg, xcol, tw);
-      __syncthreads();
+      fft_column<Plan, -1>(t, src, dst_reg, xcol, tw, zsync);
+      zsync();
 #pragma unroll
       for (int e = 0; e < E; ++e) pc[padx(pt(e))] = zr[e];
-      __syncthreads();
+      zsync();
       unpack_store(pc, zout + c * g.sY);
     }
   } else if constexpr (MODE == KZ_C2R) {
@@ -566,7 +572,7 @@ kz_kernel(const PassArgs<R> a) {
     auto dst_reg = [&](int b, int r, int, C v) { zr[b * RL + r] = v; };
     for (int f = 0; f < a.nin; ++f) {
       auto src = packed(a.in + ((long long)run * a.nin + f) * g.sY);
-      fft_column<Plan, +1>(t, src, dst_reg, xcol, tw);
+      fft_column<Plan, +1>(t, src, dst_reg, xcol, tw, zsync);
       R m = 0;
       if (a.phys_out) {
         R* po = a.phys_out + ((long long)run * a.nin + f) * g.sP + ((long long)x * N + y0) * N;
@@ -596,13 +602,13 @@ kz_kernel(const PassArgs<R> a) {
     for (int f = 0; f < a.nin; ++f) {
       const R* pi = a.phys_in + ((long long)run * a.nin + f) * g.sP + ((long long)x * N + y0) * N;
       auto src = [&](int n, int) -> C { return mk<C>(pi[n], pi[N + n]); };
-      fft_column<Plan, -1>(t, src, dst_reg, xcol, tw);
-      __syncthreads();
+      fft_column<Plan, -1>(t, src, dst_reg, xcol, tw, zsync);
+      zsync();
 #pragma unroll
       for (int e = 0; e < E; ++e) xcol[padx(out_index<Plan>(t, e / RL, e % RL))] = zr[e];
-      __syncthreads();
+      zsync();
       unpack_store(xcol, a.out + ((long long)run * a.nin + f) * g.sY);
-      __syncthreads();
+      zsync();
     }
   }
 }
@@ -636,16 +642,25 @@ static cudaError_t launch_kx(const PassArgs<R>& a, int runs, cudaStream_t st) {
   return cudaGetLastError();  // also clears a launch-configuration error
 }
 
-template <typename R, int N, int DIR>
-static cudaError_t launch_ky(const PassArgs<R>& a, int runs, cudaStream_t st) {
-  constexpr int TZ = TileZ<R, N, 3>::base;
-  constexpr int NT = YPlanFor<N>::T::P * TZ;
+template <typename R, int N, int DIR, int YC>
+static cudaError_t launch_ky_conf(const PassArgs<R>& a, int runs, cudaStream_t st) {
+  constexpr int TZ = YConf<N, YC>::TZ;
+  constexpr int NT = YConf<N, YC>::Plan::P * TZ;
   const long long smem = (long long)sizeof(cplx<R>) * (N + TZ * ColLayout<N>::CS);
-  static cudaError_t attr = set_smem(ky_kernel<R, N, DIR>, smem);
+  static cudaError_t attr = set_smem(ky_kernel<R, N, DIR, YC>, smem);
   if (attr != cudaSuccess) return attr;
   dim3 grid((a.g.Hk + TZ - 1) / TZ, N, runs * a.nin);
-  ky_kernel<R, N, DIR><<<grid, NT, smem, st>>>(a);
+  ky_kernel<R, N, DIR, YC><<<grid, NT, smem, st>>>(a);
   return cudaGetLastError();
+}
+
+// the y pass in configuration a.yconf (FP32 plans; FP64 plans use the default)
+template <typename R, int N, int DIR, int YC = 0>
+static cudaError_t launch_ky(const PassArgs<R>& a, int runs, cudaStream_t st) {
+  if constexpr (YC + 1 < YConfCount<N>::value && sizeof(R) == 4) {
+    if (a.yconf > YC) return launch_ky<R, N, DIR, YC + 1>(a, runs, st);
+  }
+  return launch_ky_conf<R, N, DIR, YC>(a, runs, st);
 }
 
 template <typename R, int N, int MODE>

@@ -35,12 +35,14 @@ template <> struct RegPlan<32> { using T = FftPlan<32, 4, 8, 4>; };
 template <> struct RegPlan<64> { using T = FftPlan<64, 8, 8, 8>; };
 template <> struct RegPlan<128> { using T = FftPlan<128, 16, 8, 2, 8>; };
 template <> struct RegPlan<256> { using T = FftPlan<256, 32, 8, 4, 8>; };
-template <> struct RegPlan<96> { using T = FftPlan<96, 8, 4, 4, 6>; };  // E = 12: x pass only
+template <> struct RegPlan<96> { using T = FftPlan<96, 8, 4, 4, 6>; };  // E = 12: x and hydro z passes
 
 // sizes with a register-resident z pass (E = 8; N = 8 has fewer line pairs than one
 // CTA holds) and with a register-resident x pass
 template <int N> struct HasRegZ { static constexpr bool value = (N == 16 || N == 32 || N == 64 || N == 128 || N == 256); };
 template <int N> struct HasRegX { static constexpr bool value = HasRegZ<N>::value || N == 96; };
+// the hydro z pass also at N = 96 (E = 12, two CTAs per SM)
+template <int N> struct HasRegZHydro { static constexpr bool value = HasRegZ<N>::value || N == 96; };
 
 // 16-byte asynchronous global -> shared copy (L1 bypass) and its completion wait
 __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
@@ -66,10 +68,12 @@ struct KzRegShape {
   // per pair: exchange column + the two spectral rows of the six input fields
   static constexpr long long per_pair = CS + 6LL * 2 * HZMAX;
   static constexpr long long smem = (long long)sizeof(cplx<R>) * (N + (long long)LP * per_pair);
+  // resident CTAs per SM the registers must allow: E = 12 holds 84 complex values a thread
+  static constexpr int MINB = (E > 8) ? 2 : 3;
 };
 
 template <typename R, int N>
-__global__ void __launch_bounds__(128, 3) kz_reg_kernel(const PassArgs<R> a) {
+__global__ void __launch_bounds__(128, KzRegShape<R, N>::MINB) kz_reg_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Sh = KzRegShape<R, N>;
   using Plan = typename Sh::Plan;
@@ -596,6 +600,9 @@ struct KxRegShape {
   static constexpr int NT = NG * GT;
   // resident CTAs per SM the registers must allow (E = 12 at N = 96 needs ~168 registers)
   static constexpr int MINB = (NT >= 256) ? 2 : ((E > 8) ? 3 : 4);
+  // kz-fastest grid order: measured 161 -> 156 us at 256^3; no gain at 128^3, slower in the
+  // batched 96^3 group
+  static constexpr bool KZ_FAST = (N >= 256);
   static constexpr int PSH = 3;
   // exchange column stride: = 4 (mod 16) for 4-column groups, = 2 for 8 (bank-conflict model)
   static constexpr int CS = ColLayout<N, PSH, (QW == 8) ? 2 : 4>::CS;
@@ -641,8 +648,12 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
   C* tw = reinterpret_cast<C*>(smem_raw);
   const int grp = threadIdx.x / GT, lt = threadIdx.x % GT;
   const int col = lt % QW, t = lt / QW;
-  const int iyc = blockIdx.x, run = blockIdx.z;
-  const int kz0 = (blockIdx.y * Sh::NG + grp) * QW;
+  // grid (Sh::KZ_FAST): (kz blocks, ky rows, runs), so that CTAs launched together take
+  // adjacent kz of one ky row and their row segments of W, X, S and A adjoin in memory;
+  // else (ky rows, kz blocks, runs)
+  const int bky = Sh::KZ_FAST ? blockIdx.y : blockIdx.x, bkz = Sh::KZ_FAST ? blockIdx.x : blockIdx.y;
+  const int iyc = bky, run = blockIdx.z;
+  const int kz0 = (bkz * Sh::NG + grp) * QW;
   const int kz = kz0 + col;
   const bool zok = kz < g.Hk;
   C* xcol = tw + N + (grp * QW + col) * CS;
@@ -683,7 +694,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
         const R kx = R(ksigned(i, K));
         k2 = kx * kx;
       } else {
-        const R kc = R(blockIdx.y * Sh::NG * QW + (i - M));  // kz of column i - M
+        const R kc = R(bkz * Sh::NG * QW + (i - M));  // kz of column i - M
         k2 = R(kyf * kyf) + kc * kc;
       }
       ftab[i] = mk<C>(rexpm1<R>(-c1 * k2), rexpm1<R>(-ch * k2));
@@ -1323,7 +1334,8 @@ static cudaError_t launch_kx_reg(const PassArgs<R>& a, int runs, cudaStream_t st
   static cudaError_t attr = set_smem(kx_reg_kernel<R, N, MODE>, Sh::smem);
   if (attr != cudaSuccess) return attr;
   const int quads = (a.g.Hk + Sh::QW - 1) / Sh::QW;
-  dim3 grid(a.g.M, (quads + Sh::NG - 1) / Sh::NG, runs);
+  const int kzb = (quads + Sh::NG - 1) / Sh::NG;
+  const dim3 grid = Sh::KZ_FAST ? dim3(kzb, a.g.M, runs) : dim3(a.g.M, kzb, runs);
   kx_reg_kernel<R, N, MODE><<<grid, Sh::NT, Sh::smem, st>>>(a);
   return cudaGetLastError();
 }

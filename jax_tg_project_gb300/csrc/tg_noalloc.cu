@@ -14,6 +14,13 @@
 // call overwrites every slot it reads, so nothing needs clearing.  Calls that
 // overlap on the GPU (different streams, or host threads racing on one device)
 // race on the array and must be ordered by the caller.
+//
+// The array's device address is looked up (cudaGetSymbolAddress) on the first
+// call in each CUDA context, with that context current, and cached under the
+// context's unique id: a device reset, or a context other than the primary one,
+// loads the module again at a new address, and the next call then looks it up
+// again instead of handing a stale address to the kernels.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -25,6 +32,7 @@
 
 namespace tg {
 void set_last_error(const std::string& message);  // tg_api.cu
+bool size_built(int n, int prec);                  // tg_api.cu
 }
 
 namespace {
@@ -32,13 +40,22 @@ namespace {
 constexpr int kBlocks = 96;   // partial sums per run
 constexpr int kThreads = 256;
 constexpr int kQ = 5;         // E_k, enstrophy, sum w k^2 |u|^2, E_m, H_c
-constexpr int kMaxDevices = 64;
+constexpr int kMaxContexts = 64;
 
 static __device__ __align__(256) double g_partials[TG_NOALLOC_MAX_RUNS * kBlocks * kQ];
 
-// host copy of the array's device address, looked up once per device
+// host copies of the array's device address, one per CUDA context (keyed by the
+// context's unique id), most recent first
 std::mutex g_mu;
-double* g_addr[kMaxDevices] = {nullptr};
+struct CtxAddr {
+  unsigned long long id = 0;
+  double* addr = nullptr;
+};
+CtxAddr g_addr[kMaxContexts];
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_id = nullptr;
 
 
 struct Comp {
@@ -106,21 +123,49 @@ int fail(int code, const std::string& m) {
   return code;
 }
 
-// the device address of g_partials for the current device (looked up once)
+// the device address of g_partials in the current context (looked up once per context)
 int partials_address(double** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fail(TG_E_CUDA, std::string("tg_diagnostics_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return fail(TG_E_UNSUPPORTED, "tg_diagnostics_noalloc: device index too large");
+  cudaError_t e;
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
+  if (!g_ctx_current || !g_ctx_id) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return fail(TG_E_CUDA, "tg_diagnostics_noalloc: the driver does not provide cuCtxGetCurrent / cuCtxGetId");
+    g_ctx_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    g_ctx_id = reinterpret_cast<CtxGetIdFn>(f2);
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_current(&ctx) != CUDA_SUCCESS)
+    return fail(TG_E_CUDA, "tg_diagnostics_noalloc: cuCtxGetCurrent failed");
+  if (!ctx) {  // no context yet: the runtime binds the device's primary context on this call
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_partials);
-    if (e != cudaSuccess || !p)
+    if (e != cudaSuccess)
       return fail(TG_E_CUDA, std::string("tg_diagnostics_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_addr[dev] = static_cast<double*>(p);
+    if (g_ctx_current(&ctx) != CUDA_SUCCESS || !ctx)
+      return fail(TG_E_CUDA, "tg_diagnostics_noalloc: no current CUDA context");
   }
-  *out = g_addr[dev];
+  if (g_ctx_id(ctx, &id) != CUDA_SUCCESS)
+    return fail(TG_E_CUDA, "tg_diagnostics_noalloc: cuCtxGetId failed");
+  for (int i = 0; i < kMaxContexts; ++i) {
+    if (g_addr[i].addr && g_addr[i].id == id) {
+      *out = g_addr[i].addr;
+      return TG_OK;
+    }
+  }
+  void* p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_partials);
+  if (e != cudaSuccess || !p)
+    return fail(TG_E_CUDA, std::string("tg_diagnostics_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  for (int i = kMaxContexts - 1; i > 0; --i) g_addr[i] = g_addr[i - 1];  // oldest entry drops out
+  g_addr[0].id = id;
+  g_addr[0].addr = static_cast<double*>(p);
+  *out = g_addr[0].addr;
   return TG_OK;
 }
 
@@ -130,11 +175,16 @@ extern "C" int tg_diagnostics_noalloc(const void* state, int n, int batch, int p
                                       double eta, double* out, void* stream) {
   (void)eta;
   if (!state || !out) return fail(TG_E_INVALID, "tg_diagnostics_noalloc: null argument");
-  if (n < 4) return fail(TG_E_INVALID, "tg_diagnostics_noalloc: n must be at least 4");
   if (physics != TG_PHYS_HYDRO && physics != TG_PHYS_MHD)
     return fail(TG_E_INVALID, "tg_diagnostics_noalloc: physics must be TG_PHYS_HYDRO or TG_PHYS_MHD");
   if (precision != TG_PREC_F32 && precision != TG_PREC_F64)
     return fail(TG_E_INVALID, "tg_diagnostics_noalloc: precision must be TG_PREC_F32 or TG_PREC_F64");
+  // only the sizes tg_plan_create accepts: their states are the only buffers laid out this way
+  if (!tg::size_built(n, precision))
+    return fail(TG_E_UNSUPPORTED, "tg_diagnostics_noalloc: grid size " + std::to_string(n) +
+                                      " is not built for this precision");
+  // there is no plan whose nu a negative value could select: nu is used as given
+  if (!(nu >= 0.0)) return fail(TG_E_INVALID, "tg_diagnostics_noalloc: nu must be nonnegative");
   if (batch < 1 || batch > TG_NOALLOC_MAX_RUNS)
     return fail(TG_E_INVALID, "tg_diagnostics_noalloc: batch " + std::to_string(batch) +
                                   " is outside 1.." + std::to_string(TG_NOALLOC_MAX_RUNS) +

@@ -32,8 +32,10 @@ class Plan:
 
     def __init__(self, n, batch=1, physics="hydro", precision="f32", explicit_viscosity=False,
                  lorentz_sign=1.0, cutoff=0, device=None, autotune=False):
-        """``autotune``: time the register-resident and shared-memory pass variants on this
-        shape when the plan is created and keep the fastest (``variant``)."""
+        """``autotune``: time the register-resident and shared-memory pass variants, then the
+        y-pass configurations, on this shape and batch when the plan is created and keep the
+        fastest (``variant``, ``y_config``; TG_AUTOTUNE_CACHE names a file that keeps the
+        choices across processes)."""
         if not torch.cuda.is_available():
             raise RuntimeError("jax_tg_project_gb300 needs a CUDA device (no CPU path exists)")
         self.lib = _abi.load()
@@ -97,6 +99,14 @@ class Plan:
     def variant(self):
         """Pass variant in use: bit 0 = shared-memory z passes, bit 1 = shared-memory x passes."""
         return int(self.lib.tg_pass_variant(self._h))
+
+    @property
+    def y_config(self):
+        """(configuration in use, configurations built) of the y pass: radix plan and kz
+        columns per CTA, chosen by ``autotune`` (0 = the default)."""
+        count = ctypes.c_int(0)
+        cur = int(self.lib.tg_y_config(self._h, ctypes.byref(count)))
+        return cur, int(count.value)
 
     @property
     def last_launch_count(self):

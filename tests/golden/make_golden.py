@@ -14,7 +14,9 @@ script imports the reference modules unchanged with small stand-ins:
 The arithmetic that runs is therefore the reference's, with NumPy/SciPy FP64
 FFTs in place of XLA/cuFFT.  Inputs are seeded.  Usage (writes *.npz here):
 
-    python tests/golden/make_golden.py [--reference /root/reference] [--skip-64]
+    python tests/golden/make_golden.py --reference <reference checkout> [--skip-64]
+
+(or set TG_REFERENCE_DIR to the checkout instead of passing --reference)
 """
 from __future__ import annotations
 
@@ -202,9 +204,12 @@ def cupy_packages(ref_root):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("TG_REFERENCE_DIR"),
+                    help="root of the reference checkout (default: $TG_REFERENCE_DIR)")
     ap.add_argument("--skip-64", action="store_true")
     a = ap.parse_args()
+    if not a.reference:
+        ap.error("the reference checkout is required: --reference DIR or TG_REFERENCE_DIR")
     _install_stand_ins()
     os.chdir(HERE)  # run_simulation prints; nothing is written by the stand-in plots
     hydro(a.reference, a.skip_64)

@@ -111,7 +111,7 @@ def test_batched_runs_are_independent():
         assert torch.equal(s1[0], sb[r])
 
 
-@pytest.mark.parametrize("N", [16, 32, 64, 128])
+@pytest.mark.parametrize("N", [16, 32, 64, 96, 128])
 def test_register_and_shared_memory_passes_agree(N, monkeypatch):
     """The register-resident x/z passes and the shared-memory passes are two
     implementations of the same step; every mix of them (TG_PASS_VARIANT bit 0: z, bit 1:
@@ -230,3 +230,46 @@ def test_run_in_chunks_matches_step(physics):
     assert torch.equal(a, b)
     d = p.diagnostics(b, nu=0.004, eta=0.003)
     assert torch.equal(series[-1], d)
+
+
+@pytest.mark.parametrize("N", [32, 64, 128, 256])
+def test_y_configurations_agree(N, monkeypatch):
+    """Every y-pass configuration (radix plan, kz columns per CTA) the autotuner may pick
+    gives the default configuration's step to FP32 round-off."""
+    import jax_tg_project_gb300 as tg
+    monkeypatch.delenv("TG_PASS_VARIANT", raising=False)
+    count = tg.Plan(N, precision="f32").y_config[1]
+    assert count >= 2
+    outs = []
+    for y in range(count):
+        monkeypatch.setenv("TG_Y_CONF", str(y))
+        p = tg.Plan(N, precision="f32")
+        assert p.y_config == (y, count)
+        s = p.initial_condition("taylor_green", seed=9, pert_amp=0.05, k0=3.0)
+        p.step(s, dt=2e-3, nu=2e-3, nsteps=2)
+        outs.append(from_state(p, s)[0])
+    for y in range(1, count):
+        assert rel_l2(outs[0], outs[y]) < 2e-6, y
+
+
+def test_autotune_cache_is_written_and_read(tmp_path, monkeypatch):
+    """TG_AUTOTUNE_CACHE: a tuned plan appends its choice; a later plan of the same key takes
+    the cached choice instead of timing (shown by editing the cached values)."""
+    import jax_tg_project_gb300 as tg
+    monkeypatch.delenv("TG_PASS_VARIANT", raising=False)
+    monkeypatch.delenv("TG_Y_CONF", raising=False)
+    cache = tmp_path / "tune.txt"
+    monkeypatch.setenv("TG_AUTOTUNE_CACHE", str(cache))
+    p = tg.Plan(64, batch=2, precision="f32", autotune=True)
+    lines = cache.read_text().splitlines()
+    assert len(lines) == 1 and " n=64 batch=2 " in lines[0]
+    assert lines[0].endswith(f"variant={p.variant} yconf={p.y_config[0]}")
+    forced_v, forced_y = (p.variant + 1) % 4, (p.y_config[0] + 1) % p.y_config[1]
+    key = lines[0][: lines[0].index(" variant=")]
+    cache.write_text(lines[0] + "\n" + f"{key} variant={forced_v} yconf={forced_y}\n")
+    q = tg.Plan(64, batch=2, precision="f32", autotune=True)
+    assert (q.variant, q.y_config[0]) == (forced_v, forced_y)
+    assert len(cache.read_text().splitlines()) == 2  # a cache hit appends nothing
+    r = tg.Plan(64, batch=3, precision="f32", autotune=True)  # another key: tuned and appended
+    assert len(cache.read_text().splitlines()) == 3
+    del p, q, r

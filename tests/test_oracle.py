@@ -235,3 +235,34 @@ def test_compact_layout_round_trip_and_parseval(N):
     assert ke == pytest.approx(T.kinetic_energy(u), rel=1e-12)
     assert ens == pytest.approx(T.enstrophy(u, kx, ky, kz), rel=1e-12)
     assert diss == pytest.approx(T.viscous_dissipation(u, 0.01, kx, ky, kz), rel=1e-12)
+
+
+# ------------------------------------------------------------------ torch restatement pins
+def test_torch_restatement_matches_reference(golden_hydro):
+    """oracle/tg_torch.py (the reverse-mode reference for the adjoint tests) against the
+    reference's own outputs: RHS and one RK4 step at 16^3, the enstrophy of the Taylor-Green
+    state, and the run series (jax/taylor_green_jax.py:158-201, run8 / run16 cases)."""
+    import torch
+
+    from oracle import tg_torch as TT
+    g = golden_hydro
+    kx, ky, kz, mask = TT._grid(16)
+    uin = torch.from_numpy(np.asarray(g["rhs16_in"], dtype=np.float64))
+    assert rel_l2(TT.spectral_rhs(uin, 0.01, kx, ky, kz, mask).numpy(), g["rhs16_out"]) < 1e-13
+    assert rel_l2(TT.advance_one_step(uin, 0.005, 0.01, kx, ky, kz, mask).numpy(),
+                  g["step16_out"]) < 1e-14
+    u0 = torch.from_numpy(T.initial_taylor_green(16))
+    assert float(TT.enstrophy(u0, kx, ky, kz)) == pytest.approx(float(g["ic16_enstrophy"]), rel=1e-13)
+    for case, N, nu, nsteps in (("run8", 8, 0.01, 4), ("run16", 16, 2 * np.pi / 100, 10)):
+        kx, ky, kz, mask = TT._grid(N)
+        u = torch.from_numpy(T.initial_taylor_green(N))
+        ens = [float(TT.enstrophy(u, kx, ky, kz))]
+        for s in range(nsteps):
+            u = TT.advance_one_step(u, 0.005, nu, kx, ky, kz, mask)
+            if (s + 1) % 2 == 0:
+                ens.append(float(TT.enstrophy(u, kx, ky, kz)))
+        np.testing.assert_allclose(ens, g[f"{case}_enstrophy"], rtol=1e-12)
+        assert rel_l2(u.numpy(), g[f"{case}_u"]) < 1e-12
+    # final_enstrophy is the composition of the two pinned pieces
+    L = TT.final_enstrophy(torch.from_numpy(T.initial_taylor_green(8)), 0.01, 0.005, 4)
+    assert float(L) == pytest.approx(float(g["run8_enstrophy"][-1]), rel=1e-12)
