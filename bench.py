@@ -188,8 +188,9 @@ class _DevicePeak:
 def measure_adjoint(n=128, nsteps=256):
     """Gradient of the final enstrophy (128^3 FP32 hydro, TG + 1e-2 perturbation,
     nu = 1/1600, dt = 1e-3, 256 steps): time of the hand-written adjoint relative to the
-    forward run and its device memory, for the stage tape in pinned host memory (the
-    default) and for sqrt(n) checkpointing with segment recompute."""
+    forward run and its memory, for the stage tape of the whole run in pinned host memory
+    and for sqrt(n) checkpointing (each segment recomputed from its checkpoint with its
+    tape recorded, then swept backwards)."""
     import math
 
     import torch
@@ -225,21 +226,33 @@ def measure_adjoint(n=128, nsteps=256):
     for mode, arg in (("tape", "tape"), ("checkpoint", ck)):
         # timed alone: the memory sampler's driver calls would slow the adjoint's host loop
         # (it enqueues the tape transfers and step graphs while the device runs)
-        t_adj, adj_all, res = timed(lambda: plan.adjoint(s0, 1e-3, 1 / 1600, nsteps, arg))
+        phases = []
+
+        def call():
+            r = plan.adjoint(s0, 1e-3, 1 / 1600, nsteps, arg)
+            phases.append(plan.adjoint_profile())
+            return r
+        t_adj, adj_all, res = timed(call)
         loss, grad, gnu = res
         with _DevicePeak() as mp:  # the same call again for its device memory
             plan.adjoint(s0, 1e-3, 1 / 1600, nsteps, arg)
             torch.cuda.synchronize()
         # adjoint memory = the forward's + the call's own device buffers (sampled) + the
-        # initial state and gradient it reads and returns
+        # initial state and gradient it reads and returns; the pinned host memory the call
+        # keeps (the tape of the whole run, or of one segment plus the segment checkpoints
+        # and the parked adjoint state) is reported beside it and in a second ratio
         adj_mem = fwd_mem + mp.peak + 2 * f
+        seg = nsteps if mode == "tape" else ck
+        nseg = -(-nsteps // seg)
+        host = (4 * seg + (nseg + 1 if nseg > 1 else 0)) * f
         out[mode] = {"adjoint_ms": t_adj, "adjoint_ms_all": adj_all, "time_ratio": t_adj / t_fwd,
-                     "adjoint_bytes": adj_mem,
-                     "memory_ratio": adj_mem / fwd_mem, "loss": float(loss), "grad_nu": float(gnu)}
+                     "time_ratio_all": [t / t_fwd for t in adj_all], "phases_ms": phases,
+                     "adjoint_bytes": adj_mem, "host_tape_bytes": host,
+                     "memory_ratio": adj_mem / fwd_mem,
+                     "memory_ratio_with_host": (adj_mem + host) / fwd_mem,
+                     "loss": float(loss), "grad_nu": float(gnu)}
         if mode == "checkpoint":
             out[mode]["checkpoint_every"] = ck
-        else:
-            out[mode]["host_tape_bytes"] = 4 * nsteps * f
     out["time_ratio"] = out["tape"]["time_ratio"]
     out["memory_ratio"] = out["tape"]["memory_ratio"]
     return out

@@ -213,16 +213,27 @@ int64_t tg_last_launch_count(const tg_plan* plan);
  * t_final).  Writes loss (device double), grad_state = dloss/dstate0 (device, state
  * layout; the gradient for the inner product sum_half w Re(a conj b), w = 1 at
  * kz = 0 and 2 otherwise) and grad_nu = dloss/dnu (device double).
- * checkpoint_every > 0: states are checkpointed every checkpoint_every steps and each
- * segment is recomputed on the way back; 0: every ceil(sqrt(nsteps)) steps.
- * TG_ADJ_HOST_TAPE: one forward sweep records every step's state and stage nonlinear
- * terms in pinned host memory (4 states per step, kept by the plan for later calls) and
- * nothing is recomputed; FP32 plans with register passes (n = 16 ... 256), else (or if
- * the host memory cannot be pinned) the sqrt(nsteps) checkpointing runs instead.
+ * checkpoint_every > 0: states are checkpointed every checkpoint_every steps (0: every
+ * ceil(sqrt(nsteps)) steps) and each segment is recomputed on the way back.  With the
+ * stage-tape kernels (FP32 plans with register passes, n = 16 ... 256) the recompute of a
+ * segment records its step tape (the step's state and stage nonlinear terms, 4 states per
+ * step) in pinned host memory and the backward sweep reads it; the checkpoints and the
+ * adjoint state are held in pinned host memory meanwhile (the plan keeps that memory for
+ * later calls), so the device holds only the plan, the working state and 8 tape states.
+ * Other plans recompute each step's stage terms on the device.
+ * TG_ADJ_HOST_TAPE: one forward sweep records the tape of every step in pinned host
+ * memory and nothing is recomputed (with the stage-tape kernels; else, or if the host
+ * memory cannot be pinned, the sqrt(nsteps) checkpointing runs instead).
  * The reference has no adjoint; its autodiff counterpart is jax.grad through
  * jax/taylor_green_jax.py:188-196.  Allocates its device work buffers for the call and
  * synchronises the stream. */
 #define TG_ADJ_HOST_TAPE (-1)
+
+/* Phases of the plan's last stage-tape tg_adjoint call, in ms of device time (CUDA events on
+ * the plan's stream): ms[0] the forward run (with the tape recorded, or keeping the segment
+ * checkpoints) and the loss, ms[1] the tape recording sweeps of the segments (0 for the
+ * whole-run tape), ms[2] the backward sweeps.  No reference counterpart. */
+int tg_adjoint_profile(const tg_plan* plan, double ms[3]);
 
 /* Free the pinned host memory a TG_ADJ_HOST_TAPE adjoint keeps in the plan for later calls
  * (the plan stays usable; the next tape adjoint pins it again).  No reference counterpart. */

@@ -70,6 +70,7 @@ SIGNATURES = {
     "tg_pass_variant": (c_int, [c_void_p]),
     "tg_y_config": (c_int, [c_void_p, ctypes.POINTER(c_int)]),
     "tg_release_host_tape": (c_int, [c_void_p]),
+    "tg_adjoint_profile": (c_int, [c_void_p, ctypes.POINTER(c_double)]),
     "tg_last_error": (ctypes.c_char_p, []),
     "tg_version": (c_int, []),
 }

@@ -673,6 +673,9 @@ struct tg_plan {
   int nyconf = 1;   // configurations built for this size and precision
   // per-launch CUDA events (op, start, stop) while tg_profile_passes runs
   std::vector<ProfEvent>* prof = nullptr;
+  // phases of the last stage-tape adjoint (tg_adjoint_profile): forward run, tape recording
+  // sweeps of the segments, backward sweeps (ms, CUDA events on the plan's stream)
+  double adj_ms[3] = {0.0, 0.0, 0.0};
 };
 
 namespace {
@@ -1237,6 +1240,12 @@ int tg_plan_create(tg_plan** out, const tg_desc* d) {
 
 int tg_pass_variant(const tg_plan* p) { return p ? p->variant : 0; }
 
+int tg_adjoint_profile(const tg_plan* p, double ms[3]) {
+  if (!p || !ms) return fail(TG_E_INVALID, "tg_adjoint_profile: null argument");
+  for (int i = 0; i < 3; ++i) ms[i] = p->adj_ms[i];
+  return TG_OK;
+}
+
 int tg_y_config(const tg_plan* p, int* count) {
   if (count) *count = p ? p->nyconf : 0;
   return p ? p->yconf : 0;
@@ -1784,13 +1793,27 @@ struct Adjoint {
     a.nout = 9;
     return Ops<R>::go(p, op, a, "kx adjoint");
   }
-  int run_tape(const void* state0, double dt, double nu, int nsteps, void* grad, double* grad_nu, double* loss) {
+  // The stage-tape adjoint.  seglen >= nsteps: one forward sweep records the tape of every
+  // step in pinned host memory, and the backward sweep reads it back.  seglen < nsteps
+  // (sqrt(n) checkpointing): a forward sweep keeps the state at the start of every segment
+  // of seglen steps (pinned host memory); the segments are then taken last to first, each
+  // recomputed from its checkpoint with its tape recorded (seglen steps of tape in host
+  // memory) and swept backwards.  While a segment is recomputed, lam (whose device buffer
+  // is a tape slot then) is parked in host memory.  Device memory beyond the plan is the
+  // same in both schedules: the two tape slots (eight states, the backward buffers V x 2,
+  // n1, n2, n3, lam x 2, g), the working state and the partial sums.
+  int run_tape(const void* state0, double dt, double nu, int nsteps, int seglen, void* grad, double* grad_nu,
+               double* loss) {
     int rc;
     const Geo& g = p->g;
     cudaStream_t st = p->st;
     fbytes = sizeof(C) * 3 * (size_t)g.sS;
     const size_t sN = 3 * (size_t)g.sS;  // elements of one state
-    const size_t need = (size_t)nsteps * 4 * fbytes;
+    seglen = std::max(1, std::min(seglen, nsteps));
+    const int nseg = (nsteps + seglen - 1) / seglen;
+    const size_t tape_states = (size_t)seglen * 4;
+    const size_t extra_states = (nseg > 1) ? (size_t)nseg + 1 : 0;  // checkpoints, parked lam
+    const size_t need = (tape_states + extra_states) * fbytes;
     if (p->htape_bytes < need) {
       if (p->htape) cudaFreeHost(p->htape);
       p->htape = nullptr;
@@ -1799,11 +1822,13 @@ struct Adjoint {
       if (e != cudaSuccess) {
         (void)cudaGetLastError();
         p->htape = nullptr;
-        return TG_E_NOMEM;  // the caller falls back to checkpointing
+        return TG_E_NOMEM;  // the caller falls back to recomputing the stage terms
       }
       p->htape_bytes = need;
     }
     C* host = static_cast<C*>(p->htape);
+    C* hck = host + tape_states * sN;    // segment checkpoints
+    C* hlam = hck + (size_t)nseg * sN;   // lam while a segment is recomputed
     C *slot = nullptr, *cur0 = nullptr;
     if ((rc = alloc((void**)&slot, 8 * fbytes))) return rc;
     if ((rc = alloc((void**)&cur0, fbytes))) return rc;
@@ -1814,12 +1839,25 @@ struct Adjoint {
     const size_t pslots = (size_t)g.M * ((g.Hk + 3) / 4);
     if ((rc = alloc((void**)&dpart, sizeof(double) * 3 * pslots))) return rc;
     TG_CUDA(cudaMemsetAsync(dpart, 0, sizeof(double) * 3 * pslots, st), "memset");
+    TG_CUDA(cudaMemsetAsync(dnu, 0, sizeof(double), st), "memset");
     blocks = (int)std::min<long long>(((long long)g.M * g.M * g.Hk + 255) / 256, 2048);
     TG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "copy stream");
     cudaEvent_t written[2] = {event(), event()}, copied[2] = {event(), event()};
+    // refill events: a tape buffer is reloaded as soon as its last reader has run
+    //   n3 (stage-4 nu terms), n2 (stage-3 state), n1 (stage-2 nu terms), V (stage-1 state)
+    cudaEvent_t n3_free = event(), n2_free = event(), n1_free = event(), v_free[2] = {event(), event()};
+    cudaEvent_t n3_ready = event(), n2_ready = event(), n1_ready = event(), v_ready[2] = {event(), event()};
     for (cudaEvent_t e : evs)
       if (!e) return fail(TG_E_CUDA, "tg_adjoint: event creation failed");
     C* tslot[2] = {slot, slot + 4 * sN};
+    // backward buffers (the tape slots once offloaded)
+    C* Vb[2] = {slot, slot + sN};
+    C* N1 = slot + 2 * sN;
+    C* N2 = slot + 3 * sN;
+    C* N3 = slot + 4 * sN;
+    C* Lb[2] = {slot + 5 * sN, slot + 6 * sN};
+    C* Gb = slot + 7 * sN;
+
     auto offload = [&](int j, int k) -> int {
       TG_CUDA(cudaEventRecord(written[k], st), "event record");
       TG_CUDA(cudaStreamWaitEvent(cs, written[k], 0), "stream wait");
@@ -1828,48 +1866,36 @@ struct Adjoint {
       TG_CUDA(cudaEventRecord(copied[k], cs), "event record");
       return TG_OK;
     };
-    // forward sweep: step 0 eagerly (sets kernel attributes outside capture), then graphs
-    TG_CUDA(cudaMemcpyAsync(cur0, state0, fbytes, cudaMemcpyDeviceToDevice, st), "state copy");
-    if ((rc = Ops<R>::start(p, cur0))) return rc;
-    p->tape = tslot[0];
-    rc = Ops<R>::stages(p, cur0);
-    p->tape = nullptr;
-    if (rc) return rc;
-    if ((rc = offload(0, 0))) return rc;
-    if (nsteps > 1) {
-      if ((rc = capture(0, cur0, tslot[0]))) return rc;
-      if ((rc = capture(1, cur0, tslot[1]))) return rc;
-    }
-    for (int j = 1; j < nsteps; ++j) {
-      const int k = j & 1;
-      if (j >= 2) TG_CUDA(cudaStreamWaitEvent(st, copied[k], 0), "stream wait");
-      TG_CUDA(cudaGraphLaunch(gx[k], st), "tape graph launch");
-      p->launches += 16;
-      if ((rc = offload(j, k))) return rc;
-    }
-    // loss and its gradient; the slots become the backward buffers once offloaded
-    if ((rc = Ops<R>::diagnostics(p, cur0, p->dtmp))) return rc;
-    copy_double<<<1, 32, 0, st>>>(p->dtmp + TG_D_ENSTROPHY, loss);
-    TG_CUDA(cudaStreamWaitEvent(st, copied[0], 0), "stream wait");
-    TG_CUDA(cudaStreamWaitEvent(st, copied[1], 0), "stream wait");
-    C* Vb[2] = {slot, slot + sN};
-    C* N1 = slot + 2 * sN;
-    C* N2 = slot + 3 * sN;
-    C* N3 = slot + 4 * sN;
-    C* L = slot + 5 * sN;
-    C* LA = slot + 6 * sN;
-    C* Gb = slot + 7 * sN;
-    enstrophy_grad_kernel<R><<<blocks, 256, 0, st>>>(cur0, L, g);
-    TG_CUDA(cudaMemsetAsync(dnu, 0, sizeof(double), st), "memset");
-    if ((rc = launch_check("loss gradient"))) return rc;
-    // refill events: a tape buffer is reloaded as soon as its last reader has run
-    //   n3 (stage-4 nu terms), n2 (stage-3 state), n1 (stage-2 nu terms), V (stage-1 state)
-    cudaEvent_t n3_free = event(), n2_free = event(), n1_free = event(), v_free[2] = {event(), event()};
-    cudaEvent_t n3_ready = event(), n2_ready = event(), n1_ready = event(), v_ready[2] = {event(), event()};
-    for (cudaEvent_t e : evs)
-      if (!e) return fail(TG_E_CUDA, "tg_adjoint: event creation failed");
-    for (cudaEvent_t e : {v_free[0], v_free[1], n1_free, n2_free, n3_free})  // the slots are free
-      TG_CUDA(cudaEventRecord(e, st), "event record");
+    // len steps of cur0 (X holding its inverse-x fields) with the x stage kernels writing
+    // V, n1, n2, n3 of step j into tape slot j % 2, each slot offloaded to host step j; the
+    // first sweep runs its first step eagerly (kernel attributes are set outside capture)
+    auto tape_forward = [&](int len) -> int {
+      int r;
+      int j0 = 0;
+      if (!gx[0]) {
+        p->tape = tslot[0];
+        r = Ops<R>::stages(p, cur0);
+        p->tape = nullptr;
+        if (r) return r;
+        if ((r = offload(0, 0))) return r;
+        j0 = 1;
+      }
+      for (int j = j0; j < len; ++j) {
+        const int k = j & 1;
+        if (!gx[0]) {
+          if ((r = capture(0, cur0, tslot[0]))) return r;
+          if ((r = capture(1, cur0, tslot[1]))) return r;
+        }
+        TG_CUDA(cudaStreamWaitEvent(st, copied[k], 0), "stream wait");  // slot k offloaded
+        TG_CUDA(cudaGraphLaunch(gx[k], st), "tape graph launch");
+        p->launches += 16;
+        if ((r = offload(j, k))) return r;
+      }
+      // the slots become the backward buffers once offloaded
+      TG_CUDA(cudaStreamWaitEvent(st, copied[0], 0), "stream wait");
+      TG_CUDA(cudaStreamWaitEvent(st, copied[1], 0), "stream wait");
+      return TG_OK;
+    };
     auto fetch = [&](int j, C* dst, int item, cudaEvent_t free_, cudaEvent_t ready) -> int {
       TG_CUDA(cudaStreamWaitEvent(cs, free_, 0), "stream wait");
       TG_CUDA(cudaMemcpyAsync(dst, host + ((size_t)j * 4 + item) * sN, fbytes, cudaMemcpyHostToDevice, cs),
@@ -1881,17 +1907,16 @@ struct Adjoint {
       for (cudaEvent_t e : es) TG_CUDA(cudaStreamWaitEvent(st, e, 0), "stream wait");
       return TG_OK;
     };
-    // one backward step of V-buffer parity q (L and lam alternate with it too), enqueued on
-    // p->st; inside a capture the buffer-free events become external record nodes
-    const int J = nsteps - 1;
-    C* Lb[2] = {L, LA};
+    // one backward step with buffer parity q (the q-th step of a segment's sweep, modulo 2:
+    // V in Vb[q], lam read from Lb[q] and written to Lb[q ^ 1]), enqueued on p->st; inside a
+    // capture the buffer-free events become external record nodes
     int kernels = 0;
     auto step_work = [&](int q, bool capturing) -> int {
       int r;
       const int64_t before = p->launches;
       const C* tp[4] = {Vb[q], N1, N2, N3};
-      const C* Lq = Lb[(J ^ q) & 1];
-      C* LAq = Lb[(J ^ q ^ 1) & 1];
+      const C* Lq = Lb[q];
+      C* LAq = Lb[q ^ 1];
       auto record = [&](cudaEvent_t e) -> int {
         TG_CUDA(cudaEventRecordWithFlags(e, p->st, capturing ? cudaEventRecordExternal : cudaEventRecordDefault),
                 "event record");
@@ -1913,14 +1938,6 @@ struct Adjoint {
       kernels = (int)(p->launches - before);
       return TG_OK;
     };
-    // refill the buffers of step j - 1 once step j's readers are done (V: the other buffer)
-    auto fetch_next = [&](int j) -> int {
-      int r;
-      if ((r = fetch(j - 1, Vb[(j - 1) & 1], 0, v_free[(j - 1) & 1], v_ready[(j - 1) & 1]))) return r;
-      if ((r = fetch(j - 1, N3, 3, n3_free, n3_ready))) return r;
-      if ((r = fetch(j - 1, N2, 2, n2_free, n2_ready))) return r;
-      return fetch(j - 1, N1, 1, n1_free, n1_ready);
-    };
     cudaGraphExec_t bx[2] = {nullptr, nullptr};
     cudaGraph_t bg[2] = {nullptr, nullptr};
     struct GraphGuard {  // the backward step graphs are released on every return path
@@ -1933,43 +1950,113 @@ struct Adjoint {
         }
       }
     } guard{bx, bg};
-    for (int j = J; j >= 0; --j) {
-      const int q = j & 1;
-      if (j == J) {
-        if ((rc = fetch(j, Vb[q], 0, v_free[q], v_ready[q]))) return rc;
-        if ((rc = fetch(j, N3, 3, n3_free, n3_ready))) return rc;
-        if ((rc = fetch(j, N2, 2, n2_free, n2_ready))) return rc;
-        if ((rc = fetch(j, N1, 1, n1_free, n1_ready))) return rc;
-      }
-      if ((rc = wait({v_ready[q], n1_ready, n2_ready, n3_ready}))) return rc;
-      if (j == J) {  // eagerly (sets the kernels' attributes outside capture), then one graph per parity
-        if ((rc = step_work(q, false))) return rc;
-        if (j > 0) {
+    // backward over the len steps of the tape in host memory; lam enters in Lb[0] and is
+    // left in Lb[0]
+    auto backward = [&](int len) -> int {
+      int r;
+      for (cudaEvent_t e : {v_free[0], v_free[1], n1_free, n2_free, n3_free})  // the slots are free
+        TG_CUDA(cudaEventRecord(e, st), "event record");
+      for (int k = 0; k < len; ++k) {
+        const int j = len - 1 - k, q = k & 1;
+        if (k == 0) {
+          if ((r = fetch(j, Vb[0], 0, v_free[0], v_ready[0]))) return r;
+          if ((r = fetch(j, N3, 3, n3_free, n3_ready))) return r;
+          if ((r = fetch(j, N2, 2, n2_free, n2_ready))) return r;
+          if ((r = fetch(j, N1, 1, n1_free, n1_ready))) return r;
+        }
+        if ((r = wait({v_ready[q], n1_ready, n2_ready, n3_ready}))) return r;
+        if (!bx[0]) {  // eagerly (sets the kernels' attributes outside capture), then one graph per parity
+          if ((r = step_work(q, false))) return r;
           if (!p->cap) TG_CUDA(cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking), "capture stream");
-          for (int k = 0; k < 2; ++k) {
+          for (int b = 0; b < 2; ++b) {
             cudaStream_t user = p->st;
             TG_CUDA(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal), "begin capture");
             const int64_t before = p->launches;
             p->st = p->cap;
-            rc = step_work(k, true);
+            r = step_work(b, true);
             p->st = user;
             p->launches = before;
-            cudaError_t e = cudaStreamEndCapture(p->cap, &bg[k]);
-            if (rc) return rc;
+            cudaError_t e = cudaStreamEndCapture(p->cap, &bg[b]);
+            if (r) return r;
             if (e != cudaSuccess) return cuda_fail(e, "adjoint end capture");
-            TG_CUDA(cudaGraphInstantiate(&bx[k], bg[k], 0), "adjoint graph instantiate");
+            TG_CUDA(cudaGraphInstantiate(&bx[b], bg[b], 0), "adjoint graph instantiate");
           }
+        } else {
+          TG_CUDA(cudaGraphLaunch(bx[q], st), "adjoint graph launch");
+          p->launches += kernels;
         }
-      } else {
-        TG_CUDA(cudaGraphLaunch(bx[q], st), "adjoint graph launch");
-        p->launches += kernels;
+        if (j > 0) {  // refill with step j - 1 once step j's readers are done (V: the other buffer)
+          const int qn = (k + 1) & 1;
+          if ((r = fetch(j - 1, Vb[qn], 0, v_free[qn], v_ready[qn]))) return r;
+          if ((r = fetch(j - 1, N3, 3, n3_free, n3_ready))) return r;
+          if ((r = fetch(j - 1, N2, 2, n2_free, n2_ready))) return r;
+          if ((r = fetch(j - 1, N1, 1, n1_free, n1_ready))) return r;
+        }
       }
-      if (j > 0 && (rc = fetch_next(j))) return rc;
+      if (len & 1) TG_CUDA(cudaMemcpyAsync(Lb[0], Lb[1], fbytes, cudaMemcpyDeviceToDevice, st), "lam copy");
+      return TG_OK;
+    };
+
+    // phase timing: a timing event before the work and after every phase
+    std::vector<cudaEvent_t> tev;
+    std::vector<int> tphase;  // phase that ends at tev[i] (i >= 1)
+    struct TevGuard {
+      std::vector<cudaEvent_t>* v;
+      ~TevGuard() {
+        for (cudaEvent_t e : *v) cudaEventDestroy(e);
+      }
+    } tev_guard{&tev};
+    auto mark = [&](int phase) -> int {
+      cudaEvent_t e = nullptr;
+      TG_CUDA(cudaEventCreate(&e), "event");
+      tev.push_back(e);
+      tphase.push_back(phase);
+      TG_CUDA(cudaEventRecord(e, st), "event record");
+      return TG_OK;
+    };
+    if ((rc = mark(-1))) return rc;
+    TG_CUDA(cudaMemcpyAsync(cur0, state0, fbytes, cudaMemcpyDeviceToDevice, st), "state copy");
+    if (nseg == 1) {  // the tape sweep is the forward run
+      if ((rc = Ops<R>::start(p, cur0))) return rc;
+      if ((rc = tape_forward(nsteps))) return rc;
+    } else {  // the forward run keeps the segment checkpoints
+      for (int c = 0; c < nseg; ++c) {
+        TG_CUDA(cudaMemcpyAsync(hck + (size_t)c * sN, cur0, fbytes, cudaMemcpyDeviceToHost, st), "checkpoint");
+        if ((rc = Ops<R>::start(p, cur0))) return rc;
+        if ((rc = advance(p, cur0, std::min(seglen, nsteps - c * seglen)))) return rc;
+      }
     }
-    L = Lb[(J ^ 0 ^ 1) & 1];  // lam after step 0
-    TG_CUDA(cudaMemcpyAsync(grad, L, fbytes, cudaMemcpyDeviceToDevice, st), "grad copy");
+    // loss = enstrophy of the final state, lam = its gradient
+    if ((rc = Ops<R>::diagnostics(p, cur0, p->dtmp))) return rc;
+    copy_double<<<1, 32, 0, st>>>(p->dtmp + TG_D_ENSTROPHY, loss);
+    enstrophy_grad_kernel<R><<<blocks, 256, 0, st>>>(cur0, Lb[0], g);
+    if ((rc = launch_check("loss gradient"))) return rc;
+    if ((rc = mark(0))) return rc;
+    if (nseg == 1) {
+      if ((rc = backward(nsteps))) return rc;
+      if ((rc = mark(2))) return rc;
+    } else {
+      for (int c = nseg - 1; c >= 0; --c) {
+        const int len = std::min(seglen, nsteps - c * seglen);
+        TG_CUDA(cudaMemcpyAsync(hlam, Lb[0], fbytes, cudaMemcpyDeviceToHost, st), "lam park");
+        TG_CUDA(cudaMemcpyAsync(cur0, hck + (size_t)c * sN, fbytes, cudaMemcpyHostToDevice, st), "checkpoint");
+        if ((rc = Ops<R>::start(p, cur0))) return rc;
+        if ((rc = tape_forward(len))) return rc;
+        TG_CUDA(cudaMemcpyAsync(Lb[0], hlam, fbytes, cudaMemcpyHostToDevice, st), "lam unpark");
+        if ((rc = mark(1))) return rc;
+        if ((rc = backward(len))) return rc;
+        if ((rc = mark(2))) return rc;
+      }
+    }
+    TG_CUDA(cudaMemcpyAsync(grad, Lb[0], fbytes, cudaMemcpyDeviceToDevice, st), "grad copy");
     TG_CUDA(cudaMemcpyAsync(grad_nu, dnu, sizeof(double), cudaMemcpyDeviceToDevice, st), "grad_nu copy");
     TG_CUDA(cudaStreamSynchronize(st), "adjoint sync");
+    for (int i = 0; i < 3; ++i) p->adj_ms[i] = 0.0;
+    for (size_t i = 1; i < tev.size(); ++i) {
+      float ms = 0.0f;
+      if (cudaEventElapsedTime(&ms, tev[i - 1], tev[i]) == cudaSuccess) p->adj_ms[tphase[i]] += ms;
+    }
+    drop_graph(p);  // the plan's step graph of the checkpoint sweep refers to cur0
     return TG_OK;
   }
 
@@ -2026,18 +2113,21 @@ extern "C" int tg_adjoint(tg_plan* p, const void* state0, double dt, double nu, 
     return fail(TG_E_INVALID, "tg_adjoint: need dt > 0, nu >= 0 and nsteps >= 1");
   if (p->flags & TG_FLAG_EXPLICIT_VISC)
     return fail(TG_E_UNSUPPORTED, "tg_adjoint: differentiates the integrating-factor RK4 only");
-  if (checkpoint_every == TG_ADJ_HOST_TAPE) {
-    if (p->prec == TG_PREC_F32 && has_reg_adjoint(p->n) && p->variant == 0) {
-      int rc = set_coefs(p, dt, nu, 0.0);
-      if (rc) return rc;
-      p->launches = 0;
-      Adjoint<float> A{p};
-      rc = A.run_tape(state0, dt, nu, nsteps, grad_state, grad_nu, loss);
-      if (rc != TG_E_NOMEM) return rc;
-      (void)cudaGetLastError();
-    }
-    checkpoint_every = 0;  // no tape kernels for this plan, or no memory for the tape
+  // segment length: the whole run for the host tape, else the checkpoint spacing
+  const int sqrt_len = (int)std::ceil(std::sqrt((double)nsteps));
+  const int tape_len = (checkpoint_every == TG_ADJ_HOST_TAPE) ? nsteps
+                       : (checkpoint_every > 0 ? checkpoint_every : sqrt_len);
+  if (p->prec == TG_PREC_F32 && has_reg_adjoint(p->n) && p->variant == 0) {
+    // the stage-tape kernels: the tape of one segment (or of the whole run) in host memory
+    int rc = set_coefs(p, dt, nu, 0.0);
+    if (rc) return rc;
+    p->launches = 0;
+    Adjoint<float> A{p};
+    rc = A.run_tape(state0, dt, nu, nsteps, tape_len, grad_state, grad_nu, loss);
+    if (rc != TG_E_NOMEM) return rc;
+    (void)cudaGetLastError();  // no pinned host memory for the tape: recompute instead
   }
+  if (checkpoint_every == TG_ADJ_HOST_TAPE) checkpoint_every = 0;
   int seglen = checkpoint_every > 0 ? checkpoint_every : (int)std::ceil(std::sqrt((double)nsteps));
   seglen = std::max(1, std::min(seglen, nsteps));
   int rc = set_coefs(p, dt, nu, 0.0);

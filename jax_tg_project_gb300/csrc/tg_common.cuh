@@ -140,6 +140,7 @@ template <typename R> struct PassArgs {
   const cplx<R>* tp[4];  // FLAG_TAPE adjoint stage kernels: the step tape V, n1, n2, n3
   cplx<R>* out2;         // KX_ADJ_LOAD_T with nout = 9: the three a = P mu fields (x-pass layout)
   double* part;          // KX_ADJ_FWD_T: per-CTA partial sums of d(loss)/d(nu) of the stage
+  int tiles;             // tiles of a persistent or tile-indexed kernel (set by its launcher)
 };
 
 // signed wavenumber of compact index i (0..M-1)

@@ -12,6 +12,7 @@
 //              C2R -> u x omega (+ j x b, u x b) -> R2C, or plain C2R / R2C.
 #pragma once
 
+#include <algorithm>
 #include <type_traits>
 
 #include "tg_common.cuh"
@@ -640,6 +641,20 @@ static cudaError_t launch_kx(const PassArgs<R>& a, int runs, cudaStream_t st) {
   dim3 grid(a.g.M, (a.g.Hk + TZ - 1) / TZ, runs);
   kx_kernel<R, N, F, MODE><<<grid, NT, smem, st>>>(a);
   return cudaGetLastError();  // also clears a launch-configuration error
+}
+
+// resident CTAs of a kernel on the whole GPU (occupancy per SM times the SMs; once per
+// process, on the device current at the first launch), or 0 if unknown
+template <typename Kern>
+static int resident_ctas(Kern kernel, int threads, long long smem) {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, (size_t)smem) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  return sms * per_sm;
 }
 
 template <typename R, int N, int DIR, int YC>

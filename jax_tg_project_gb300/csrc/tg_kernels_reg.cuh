@@ -22,6 +22,7 @@
 // four columns share each twiddle, so a read is a broadcast).
 #pragma once
 
+#include <algorithm>
 #include <type_traits>
 
 #include "tg_kernels.cuh"
@@ -600,9 +601,10 @@ struct KxRegShape {
   static constexpr int NT = NG * GT;
   // resident CTAs per SM the registers must allow (E = 12 at N = 96 needs ~168 registers)
   static constexpr int MINB = (NT >= 256) ? 2 : ((E > 8) ? 3 : 4);
-  // kz-fastest grid order: measured 161 -> 156 us at 256^3; no gain at 128^3, slower in the
-  // batched 96^3 group
-  static constexpr bool KZ_FAST = (N >= 256);
+  // the x stage runs persistent CTAs with its tiles in kz-fastest order at N >= 256 (256^3:
+  // 156 -> 149 us); at smaller N one tile per CTA in ky-fastest order measured faster (the
+  // per-tile set-up is small there, and the batched 96^3 group ran 260 -> 313 us persistent)
+  static constexpr bool PERSIST = (N >= 256);
   static constexpr int PSH = 3;
   // exchange column stride: = 4 (mod 16) for 4-column groups, = 2 for 8 (bank-conflict model)
   static constexpr int CS = ColLayout<N, PSH, (QW == 8) ? 2 : 4>::CS;
@@ -611,8 +613,10 @@ struct KxRegShape {
   static constexpr long long stage_elems = 2LL * 3 * MMAX * QW;
   // + the integrating-factor tables: (expm1(-c kx^2) for c = nu h, nu h / 2) over kx, and
   // the same of ky^2 + kz^2 for the CTA's columns
+  // (two copies of the factor tables: the persistent x stage writes a tile's while the previous
+  // tile's may still be read)
   static constexpr long long smem =
-      (long long)sizeof(cplx<R>) * (N + (long long)NG * QW * CS + (long long)NG * stage_elems + MMAX + NG * QW);
+      (long long)sizeof(cplx<R>) * (N + (long long)NG * QW * CS + (long long)NG * stage_elems + 2 * (MMAX + NG * QW));
   // adjoint kernels, per group: a ring of four [N][QW] input tiles of the forward transforms,
   // or up to two [3][M][QW] spectral tiles, both staged by cp.async
   static constexpr long long ring_elems = 4LL * N * QW;
@@ -635,6 +639,12 @@ __device__ __forceinline__ auto uw_field(const A& v, int q, float kx, float ky, 
   }
 }
 
+// The x stage is tiled by (ky row, NG * QW kz columns, run): a.tiles tiles, taken by each CTA
+// in the order blockIdx.x, + gridDim.x, ...  With Sh::PERSIST (KX_STAGE), persistent CTAs
+// take the tiles in kz-fastest order: the twiddles are built once per CTA, and while a
+// tile's inverse transforms run, the state / accumulator tiles of the CTA's next tile are
+// staged into shared memory (cp.async) and its forward inputs are prefetched into L2, so that
+// a tile starts with its operands at hand.  Otherwise one tile per CTA, ky fastest.
 template <typename R, int N, int MODE>
 __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) kx_reg_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
@@ -648,60 +658,48 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
   C* tw = reinterpret_cast<C*>(smem_raw);
   const int grp = threadIdx.x / GT, lt = threadIdx.x % GT;
   const int col = lt % QW, t = lt / QW;
-  // grid (Sh::KZ_FAST): (kz blocks, ky rows, runs), so that CTAs launched together take
-  // adjacent kz of one ky row and their row segments of W, X, S and A adjoin in memory;
-  // else (ky rows, kz blocks, runs)
-  const int bky = Sh::KZ_FAST ? blockIdx.y : blockIdx.x, bkz = Sh::KZ_FAST ? blockIdx.x : blockIdx.y;
-  const int iyc = bky, run = blockIdx.z;
-  const int kz0 = (bkz * Sh::NG + grp) * QW;
-  const int kz = kz0 + col;
-  const bool zok = kz < g.Hk;
+  const int kzb = ((g.Hk + QW - 1) / QW + Sh::NG - 1) / Sh::NG;  // kz blocks per ky row
+  constexpr bool KZF = (MODE == KX_STAGE) && Sh::PERSIST;
+  // tile -> (kz block, ky row, run)
+  auto tile_bkz = [&](int tl) { return KZF ? tl % kzb : (tl / M) % kzb; };
+  auto tile_iyc = [&](int tl) { return KZF ? (tl / kzb) % M : tl % M; };
   C* xcol = tw + N + (grp * QW + col) * CS;
   // [0] state, [1] accumulator: [3][M][QW] each
   C* stg = tw + N + Sh::NG * QW * CS + grp * Sh::stage_elems;
   // integrating factors of the Lawson stages: expm1(-c (kx^2 + q)) with c = nu h (or nu h / 2)
   // and q = ky^2 + kz^2 is expm1(a) + expm1(b) + expm1(a) expm1(b), a = -c kx^2, b = -c q, an
-  // exact identity; the kx terms (M entries) and the (ky, kz) terms of the CTA's columns are
-  // tabulated per CTA, so that no mode evaluates expm1 (the factors stay in delta form)
-  C* ftab = tw + N + Sh::NG * QW * CS + Sh::NG * Sh::stage_elems;
-  if constexpr (MODE == KX_STAGE) {
-    // stage the state (and accumulator) tiles of this group while the forward
-    // transforms run: rows of QW consecutive kz are 32-byte aligned (Hz % 4 == 0, kz0 a
-    // multiple of QW); chunks past the padded row (kz0 + 2h >= Hz) are skipped
-    if (kz0 < g.Hk) {
+  // exact identity; the kx terms (M entries) and the (ky, kz) terms of the tile's columns are
+  // tabulated per tile, so that no mode evaluates expm1 (the factors stay in delta form).
+  // Two copies, by tile parity: a tile's table is written while the previous tile's may
+  // still be read
+  C* ftab0 = tw + N + Sh::NG * QW * CS + Sh::NG * Sh::stage_elems;
+  constexpr int FT = Sh::MMAX + Sh::NG * QW;
+  // stage the state (and accumulator) tiles of this group's columns of tile (iyc, bkz, run):
+  // rows of QW consecutive kz are 32-byte aligned (Hz % 4 == 0, kz0 a multiple of QW); chunks
+  // past the padded row (kz0 + 2h >= Hz) are skipped; one commit group per call
+  auto stage_state = [&](int iyc_, int bkz_, int run_) {
+    const int kz0_ = (bkz_ * Sh::NG + grp) * QW;
+    if (kz0_ < g.Hk) {
       const int narr = (a.stage > 1) ? 2 : 1;
-      const long long base = (long long)blockIdx.z * 3 * g.sS + (long long)iyc * Hz + kz0;
+      const long long base = (long long)run_ * 3 * g.sS + (long long)iyc_ * Hz + kz0_;
       constexpr int CPR = Sh::CPR;
       const int chunks = narr * 3 * M * CPR;  // 16-byte chunks of each row segment
       for (int c = lt; c < chunks; c += GT) {
         const int h = c % CPR, row = c / CPR;  // row = (arr * 3 + f) * M + ic
-        if (kz0 + 2 * h >= Hz) continue;
+        if (kz0_ + 2 * h >= Hz) continue;
         const int arr = row / (3 * M), fi = row % (3 * M);
         const C* src = (arr == 0 ? a.S : a.acc) + base + (long long)fi * M * Hz + 2 * h;
         cp_async16(stg + (long long)row * QW + 2 * h, src);
       }
     }
     cp_async_commit();
+  };
+  int tile = blockIdx.x;
+  if constexpr (MODE == KX_STAGE) {
+    if (tile < a.tiles) stage_state(tile_iyc(tile), tile_bkz(tile), tile / (kzb * M));
   }
   build_twiddles<Plan>(tw, a.tw, threadIdx.x, Sh::NT);
-  const float kyf = float(ksigned(iyc, K)), kzf = float(kz);
-  if constexpr (MODE == KX_STAGE) {
-    const RunCoef cf0 = a.coef[run];
-    const R c1 = R(cf0.nu * cf0.dt), ch = R(0.5) * c1;
-    for (int i = threadIdx.x; i < M + Sh::NG * QW; i += Sh::NT) {
-      R k2;
-      if (i < M) {
-        const R kx = R(ksigned(i, K));
-        k2 = kx * kx;
-      } else {
-        const R kc = R(bkz * Sh::NG * QW + (i - M));  // kz of column i - M
-        k2 = R(kyf * kyf) + kc * kc;
-      }
-      ftab[i] = mk<C>(rexpm1<R>(-c1 * k2), rexpm1<R>(-ch * k2));
-    }
-  }
-  __syncthreads();
-  const long long soff = (long long)run * 3 * g.sS + (long long)iyc * Hz + kz;  // + (f*M + ic)*M*Hz
+  if constexpr (MODE != KX_STAGE) __syncthreads();
 
   C v[3][E];
   auto run_fft = [&](auto& src, auto& dst, auto dir_tag) {
@@ -714,133 +712,178 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
       fft_column<Plan, DIR, Sh::PSH, false>(t, src, dst, xcol, tw, ws);
     }
   };
-  using Fwd = std::integral_constant<int, -1>;
-  using Inv = std::integral_constant<int, +1>;
-
-  if constexpr (MODE == KX_LOAD) {
-    const C* sin_ = a.spec_in + soff;
-#pragma unroll
-    for (int f = 0; f < 3; ++f)
-#pragma unroll
-      for (int q = 0; q < E; ++q) {
-        const int ic = kcompact_slot<N, P>(t, q, K);
-        v[f][q] = (zok && ic >= 0) ? sin_[((long long)f * M + ic) * M * Hz] : czero<C>();
-      }
-  } else {
-    const R inv_n3 = R(1) / (R(N) * R(N) * R(N));
-    const C* win = a.in + (long long)run * 3 * g.sX + (long long)iyc * Hz + kz;
-    // issue the global loads of all three fields before the first transform (the
-    // first pass of thread t reads x = t + P q into slot q), so that their latency
-    // is paid once; the slots are consumed field by field
-    C pre[3][E];
-#pragma unroll
-    for (int f = 0; f < 3; ++f)
-#pragma unroll
-      for (int q = 0; q < E; ++q)
-        pre[f][q] = zok ? win[f * g.sX + (long long)(t + P * q) * M * Hz] : czero<C>();
-#pragma unroll
-    for (int f = 0; f < 3; ++f) {
-      auto src = [&](int, int q) -> C { return pre[f][q]; };
-      auto dst = [&](int b, int r, int, C val) { v[f][b + r * NBL] = cscale(val, inv_n3); };
-      run_fft(src, dst, Fwd());
-    }
-    // fused spectral pointwise stage on the modes k = t (mod P) of this column
-    cp_async_wait_all();
+  auto gsync = [&]() {
     if constexpr (GT > 32) {
       const NamedSync ns{1 + grp, GT};
       ns();
     } else {
       __syncwarp();
     }
-    const RunCoef cf = a.coef[run];
-    const bool expl = (a.flags & FLAG_EXPLICIT) != 0;
-    const R h = R(cf.dt);
-    const C fyz = ftab[M + grp * QW + col];  // the (ky, kz) terms of this column
-#pragma unroll
-    for (int q = 0; q < E; ++q) {
-      const int ic = kcompact_slot<N, P>(t, q, K);
-      if (zok && ic >= 0) {
-        const float kx = float(ksigned(ic, K));
-        const float k2 = kx * kx + kyf * kyf + kzf * kzf;
-        leray(v[0][q], v[1][q], v[2][q], kx, kyf, kzf, k2);
-        const R lin = expl ? R(cf.nu * double(k2)) : R(0);  // explicit viscosity only
-        const C fx = ftab[ic];
-        const R m1 = expm1_add(fx.x, fyz.x), mh = expm1_add(fx.y, fyz.y);
-#pragma unroll
-        for (int f = 0; f < 3; ++f) {
-          const long long o = soff + ((long long)f * M + ic) * M * Hz;
-          const C s = stg[((long long)f * M + ic) * QW + col];
-          if (a.tape != nullptr) {  // adjoint tape (batch 1): n_stage for stages 1..3, V at stage 1
-            if (a.stage <= 3) a.tape[(long long)a.stage * 3 * g.sS + o] = v[f][q];
-            if (a.stage == 1) a.tape[o] = s;
-          }
-          C acc = (a.stage > 1) ? stg[((long long)(3 + f) * M + ic) * QW + col] : czero<C>();
-          const C vs = (expl && a.stage > 1) ? a.vs[o] : s;
-          const C nv = expl ? rk4_combine<C>(a.stage, true, v[f][q], s, acc, vs, h, lin)
-                            : lawson_combine<C>(a.stage, v[f][q], s, acc, h, m1, mh);
-          if (a.stage < 4) {
-            a.acc[o] = acc;
-            if (expl) a.vs[o] = nv;
-          } else {
-            a.S[o] = nv;
-          }
-          v[f][q] = nv;
-        }
-      } else {
-#pragma unroll
-        for (int f = 0; f < 3; ++f) v[f][q] = czero<C>();
-      }
-    }
-  }
+  };
+  using Fwd = std::integral_constant<int, -1>;
+  using Inv = std::integral_constant<int, +1>;
 
-  // inverse-x of u and curl u straight from the registers.  At N >= 128 the six transforms
-  // share one FFT body (a loop over a uniform field index; the values of this thread's modes
-  // are formed first by a switch whose cases index the registers at compile time), which
-  // keeps the kernel's code small enough for the instruction cache; smaller transforms are
-  // unrolled (the loop would raise their register count and lower occupancy).
-  C* xo = a.out + (long long)run * 6 * g.sX + (long long)iyc * Hz + kz;
-  auto values = [&](auto gi_tag, C* in) {
-    constexpr int GI = decltype(gi_tag)::value;
+  for (int it = 0; tile < a.tiles; tile += gridDim.x, ++it) {
+    const int bkz = tile_bkz(tile), iyc = tile_iyc(tile), run = tile / (kzb * M);
+    const int kz0 = (bkz * Sh::NG + grp) * QW;
+    const int kz = kz0 + col;
+    const bool zok = kz < g.Hk;
+    const float kyf = float(ksigned(iyc, K)), kzf = float(kz);
+    const long long soff = (long long)run * 3 * g.sS + (long long)iyc * Hz + kz;  // + (f*M + ic)*M*Hz
+    C* ftab = ftab0 + (it & 1) * FT;
+
+    if constexpr (MODE == KX_LOAD) {
+      const C* sin_ = a.spec_in + soff;
 #pragma unroll
-    for (int q = 0; q < E; ++q) {
-      const int ic = kcompact_slot<N, P>(t, q, K);
-      in[q] = (ic < 0) ? czero<C>() : uw_field<GI>(v, q, float(ksigned(ic, K)), kyf, kzf);
-    }
-  };
-  auto inverse_of = [&](const C* in, int gi) {
-    auto src = [&](int, int q) -> C { return in[q]; };
-    C* xg = xo + gi * g.sX;
-    auto dst = [&](int, int, int x, C val) {
-      if (zok) xg[(long long)x * M * Hz] = val;
-    };
-    run_fft(src, dst, Inv());
-  };
-  if constexpr (N >= 128) {
-#pragma unroll 1
-    for (int gi = 0; gi < 6; ++gi) {
-      C in[E];
-      switch (gi) {
-        case 0: values(std::integral_constant<int, 0>(), in); break;
-        case 1: values(std::integral_constant<int, 1>(), in); break;
-        case 2: values(std::integral_constant<int, 2>(), in); break;
-        case 3: values(std::integral_constant<int, 3>(), in); break;
-        case 4: values(std::integral_constant<int, 4>(), in); break;
-        default: values(std::integral_constant<int, 5>(), in); break;
+      for (int f = 0; f < 3; ++f)
+#pragma unroll
+        for (int q = 0; q < E; ++q) {
+          const int ic = kcompact_slot<N, P>(t, q, K);
+          v[f][q] = (zok && ic >= 0) ? sin_[((long long)f * M + ic) * M * Hz] : czero<C>();
+        }
+    } else {
+      const R inv_n3 = R(1) / (R(N) * R(N) * R(N));
+      const C* win = a.in + (long long)run * 3 * g.sX + (long long)iyc * Hz + kz;
+      // issue the global loads of all three fields before the first transform (the
+      // first pass of thread t reads x = t + P q into slot q), so that their latency
+      // is paid once; the slots are consumed field by field
+      C pre[3][E];
+#pragma unroll
+      for (int f = 0; f < 3; ++f)
+#pragma unroll
+        for (int q = 0; q < E; ++q)
+          pre[f][q] = zok ? win[f * g.sX + (long long)(t + P * q) * M * Hz] : czero<C>();
+      {  // this tile's factor tables (and, on the first tile, the twiddles) before any use
+        const RunCoef cf0 = a.coef[run];
+        const R c1 = R(cf0.nu * cf0.dt), ch = R(0.5) * c1;
+        for (int i = threadIdx.x; i < M + Sh::NG * QW; i += Sh::NT) {
+          R k2;
+          if (i < M) {
+            const R kx = R(ksigned(i, K));
+            k2 = kx * kx;
+          } else {
+            const R kc = R(bkz * Sh::NG * QW + (i - M));  // kz of column i - M
+            k2 = R(kyf * kyf) + kc * kc;
+          }
+          ftab[i] = mk<C>(rexpm1<R>(-c1 * k2), rexpm1<R>(-ch * k2));
+        }
       }
-      inverse_of(in, gi);
+      __syncthreads();
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        auto src = [&](int, int q) -> C { return pre[f][q]; };
+        auto dst = [&](int b, int r, int, C val) { v[f][b + r * NBL] = cscale(val, inv_n3); };
+        run_fft(src, dst, Fwd());
+      }
+      // fused spectral pointwise stage on the modes k = t (mod P) of this column
+      cp_async_wait_all();
+      gsync();
+      const RunCoef cf = a.coef[run];
+      const bool expl = (a.flags & FLAG_EXPLICIT) != 0;
+      const R h = R(cf.dt);
+      const C fyz = ftab[M + grp * QW + col];  // the (ky, kz) terms of this column
+#pragma unroll
+      for (int q = 0; q < E; ++q) {
+        const int ic = kcompact_slot<N, P>(t, q, K);
+        if (zok && ic >= 0) {
+          const float kx = float(ksigned(ic, K));
+          const float k2 = kx * kx + kyf * kyf + kzf * kzf;
+          leray(v[0][q], v[1][q], v[2][q], kx, kyf, kzf, k2);
+          const R lin = expl ? R(cf.nu * double(k2)) : R(0);  // explicit viscosity only
+          const C fx = ftab[ic];
+          const R m1 = expm1_add(fx.x, fyz.x), mh = expm1_add(fx.y, fyz.y);
+#pragma unroll
+          for (int f = 0; f < 3; ++f) {
+            const long long o = soff + ((long long)f * M + ic) * M * Hz;
+            const C s = stg[((long long)f * M + ic) * QW + col];
+            if (a.tape != nullptr) {  // adjoint tape (batch 1): n_stage for stages 1..3, V at stage 1
+              if (a.stage <= 3) a.tape[(long long)a.stage * 3 * g.sS + o] = v[f][q];
+              if (a.stage == 1) a.tape[o] = s;
+            }
+            C acc = (a.stage > 1) ? stg[((long long)(3 + f) * M + ic) * QW + col] : czero<C>();
+            const C vs = (expl && a.stage > 1) ? a.vs[o] : s;
+            const C nv = expl ? rk4_combine<C>(a.stage, true, v[f][q], s, acc, vs, h, lin)
+                              : lawson_combine<C>(a.stage, v[f][q], s, acc, h, m1, mh);
+            if (a.stage < 4) {
+              a.acc[o] = acc;
+              if (expl) a.vs[o] = nv;
+            } else {
+              a.S[o] = nv;
+            }
+            v[f][q] = nv;
+          }
+        } else {
+#pragma unroll
+          for (int f = 0; f < 3; ++f) v[f][q] = czero<C>();
+        }
+      }
+      // the next tile: its state / accumulator tiles into the staging area (every thread of
+      // the group is past its reads of this tile's), its forward inputs into L2
+      const int next = tile + gridDim.x;
+      if (next < a.tiles) {
+        const int nbkz = tile_bkz(next), niyc = tile_iyc(next), nrun = next / (kzb * M);
+        gsync();
+        stage_state(niyc, nbkz, nrun);
+        const int nkz0 = (nbkz * Sh::NG + grp) * QW;
+        if (nkz0 < g.Hk) {
+          const C* nw = a.in + (long long)nrun * 3 * g.sX + (long long)niyc * Hz + nkz0;
+          for (int r = lt; r < 3 * N; r += GT) {  // one 32-byte row segment each
+            const C* ptr = nw + (long long)(r / N) * g.sX + (long long)(r % N) * M * Hz;
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
+          }
+        }
+      }
     }
-  } else {
-    auto inverse = [&](auto gi_tag) {
-      C in[E];
-      values(gi_tag, in);
-      inverse_of(in, decltype(gi_tag)::value);
+
+    // inverse-x of u and curl u straight from the registers.  At N >= 128 the six transforms
+    // share one FFT body (a loop over a uniform field index; the values of this thread's modes
+    // are formed first by a switch whose cases index the registers at compile time), which
+    // keeps the kernel's code small enough for the instruction cache; smaller transforms are
+    // unrolled (the loop would raise their register count and lower occupancy).
+    C* xo = a.out + (long long)run * 6 * g.sX + (long long)iyc * Hz + kz;
+    auto values = [&](auto gi_tag, C* in) {
+      constexpr int GI = decltype(gi_tag)::value;
+#pragma unroll
+      for (int q = 0; q < E; ++q) {
+        const int ic = kcompact_slot<N, P>(t, q, K);
+        in[q] = (ic < 0) ? czero<C>() : uw_field<GI>(v, q, float(ksigned(ic, K)), kyf, kzf);
+      }
     };
-    inverse(std::integral_constant<int, 0>());
-    inverse(std::integral_constant<int, 1>());
-    inverse(std::integral_constant<int, 2>());
-    inverse(std::integral_constant<int, 3>());
-    inverse(std::integral_constant<int, 4>());
-    inverse(std::integral_constant<int, 5>());
+    auto inverse_of = [&](const C* in, int gi) {
+      auto src = [&](int, int q) -> C { return in[q]; };
+      C* xg = xo + gi * g.sX;
+      auto dst = [&](int, int, int x, C val) {
+        if (zok) xg[(long long)x * M * Hz] = val;
+      };
+      run_fft(src, dst, Inv());
+    };
+    if constexpr (N >= 128) {
+#pragma unroll 1
+      for (int gi = 0; gi < 6; ++gi) {
+        C in[E];
+        switch (gi) {
+          case 0: values(std::integral_constant<int, 0>(), in); break;
+          case 1: values(std::integral_constant<int, 1>(), in); break;
+          case 2: values(std::integral_constant<int, 2>(), in); break;
+          case 3: values(std::integral_constant<int, 3>(), in); break;
+          case 4: values(std::integral_constant<int, 4>(), in); break;
+          default: values(std::integral_constant<int, 5>(), in); break;
+        }
+        inverse_of(in, gi);
+      }
+    } else {
+      auto inverse = [&](auto gi_tag) {
+        C in[E];
+        values(gi_tag, in);
+        inverse_of(in, decltype(gi_tag)::value);
+      };
+      inverse(std::integral_constant<int, 0>());
+      inverse(std::integral_constant<int, 1>());
+      inverse(std::integral_constant<int, 2>());
+      inverse(std::integral_constant<int, 3>());
+      inverse(std::integral_constant<int, 4>());
+      inverse(std::integral_constant<int, 5>());
+    }
   }
 }
 
@@ -1329,14 +1372,17 @@ static cudaError_t launch_kz_reg(const PassArgs<R>& a, int runs, cudaStream_t st
 }
 
 template <typename R, int N, int MODE>
-static cudaError_t launch_kx_reg(const PassArgs<R>& a, int runs, cudaStream_t st) {
+static cudaError_t launch_kx_reg(const PassArgs<R>& a0, int runs, cudaStream_t st) {
   using Sh = KxRegShape<R, N>;
   static cudaError_t attr = set_smem(kx_reg_kernel<R, N, MODE>, Sh::smem);
   if (attr != cudaSuccess) return attr;
-  const int quads = (a.g.Hk + Sh::QW - 1) / Sh::QW;
-  const int kzb = (quads + Sh::NG - 1) / Sh::NG;
-  const dim3 grid = Sh::KZ_FAST ? dim3(kzb, a.g.M, runs) : dim3(a.g.M, kzb, runs);
-  kx_reg_kernel<R, N, MODE><<<grid, Sh::NT, Sh::smem, st>>>(a);
+  static const int resident = resident_ctas(kx_reg_kernel<R, N, MODE>, Sh::NT, Sh::smem);
+  PassArgs<R> a = a0;
+  const int kzb = ((a.g.Hk + Sh::QW - 1) / Sh::QW + Sh::NG - 1) / Sh::NG;
+  a.tiles = kzb * a.g.M * runs;
+  int ctas = a.tiles;  // one tile per CTA
+  if (MODE == KX_STAGE && Sh::PERSIST && resident > 0) ctas = std::min(a.tiles, resident);
+  kx_reg_kernel<R, N, MODE><<<ctas, Sh::NT, Sh::smem, st>>>(a);
   return cudaGetLastError();
 }
 

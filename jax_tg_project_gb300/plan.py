@@ -258,7 +258,8 @@ class Plan:
         """(loss, grad_state, grad_nu) of loss = final enstrophy after nsteps steps.
 
         checkpoint_every: > 0 checkpoints every that many steps and recomputes each
-        segment; 0 every ceil(sqrt(nsteps)) steps; "tape" (or -1) records every step's
+        segment (recording its stage tape in pinned host memory where the plan has the tape
+        kernels); 0 every ceil(sqrt(nsteps)) steps; "tape" (or -1) records every step's
         stage data in pinned host memory in one forward sweep and recomputes nothing.
         """
         if checkpoint_every == "tape":
@@ -271,6 +272,13 @@ class Plan:
                                   int(checkpoint_every), _ptr(grad), ctypes.c_void_p(out.data_ptr()),
                                   ctypes.c_void_p(out.data_ptr() + 8)))
         return out[1], grad, out[0]
+
+    def adjoint_profile(self):
+        """Device time (ms) of the phases of the last stage-tape ``adjoint`` call: the forward
+        run with the loss, the tape recording sweeps of the segments, the backward sweeps."""
+        ms = (ctypes.c_double * 3)()
+        check(self.lib.tg_adjoint_profile(self._h, ms))
+        return {"forward": ms[0], "record": ms[1], "backward": ms[2]}
 
     def release_tape(self):
         """Free the pinned host memory a ``checkpoint_every="tape"`` adjoint keeps for later calls."""

@@ -108,19 +108,19 @@ def test_adjoint_128_fp32_finite_differences():
     assert max(rel) < 3e-2, rel
 
 
-@pytest.mark.parametrize("N,nsteps", [(16, 5), (32, 9), (128, 6)])
-def test_host_tape_adjoint_matches_checkpointed(N, nsteps):
-    """The stage-tape adjoint (one forward sweep, stage data in pinned host memory, no
-    recomputation) and the checkpointed adjoint compute the same discrete gradient;
-    they differ only in FP32 rounding (stage states formed in another kernel)."""
+@pytest.mark.parametrize("N,nsteps,ck", [(16, 5, 2), (32, 9, 0), (32, 8, 3), (128, 6, 4)])
+def test_host_tape_adjoint_matches_checkpointed(N, nsteps, ck):
+    """The whole-run stage tape (one forward sweep, stage data in pinned host memory) and
+    sqrt(n) checkpointing (each segment recomputed from its checkpoint with its tape
+    recorded, segments of ck steps, 0: ceil(sqrt n), the last one shorter when ck does not
+    divide nsteps) run the same kernels on the same states: identical results."""
     p = _plan(N, "f32")
     dt, nu = 2e-3, 1 / 400
     s0 = p.initial_condition("taylor_green", seed=6, pert_amp=0.05, k0=3.0)
-    lc, gc, nc = p.adjoint(s0, dt, nu, nsteps, 2)
+    lc, gc, nc = p.adjoint(s0, dt, nu, nsteps, ck)
     lt, gt, nt = p.adjoint(s0, dt, nu, nsteps, "tape")
-    assert float(lt) == pytest.approx(float(lc), rel=1e-6)
-    assert rel_l2(from_state(p, gt), from_state(p, gc)) < 2e-5
-    assert float(nt) == pytest.approx(float(nc), rel=1e-4)
+    assert float(lt) == float(lc) and float(nt) == float(nc)
+    assert bool((gt == gc).all())
     # a second call reuses the plan's host tape; after a release the next call pins it again
     lt2, gt2, nt2 = p.adjoint(s0, dt, nu, nsteps, "tape")
     assert float(lt2) == float(lt) and float(nt2) == float(nt)
@@ -150,6 +150,23 @@ def test_host_tape_edge_cases(N, cutoff, nsteps):
     s0 = p.initial_condition("taylor_green", seed=11, pert_amp=0.05, k0=3.0)
     lc, gc, nc = p.adjoint(s0, 2e-3, 1 / 300, nsteps, 1)
     lt, gt, nt = p.adjoint(s0, 2e-3, 1 / 300, nsteps, "tape")
-    assert float(lt) == pytest.approx(float(lc), rel=1e-6)
-    assert rel_l2(from_state(p, gt), from_state(p, gc)) < 2e-5
-    assert float(nt) == pytest.approx(float(nc), rel=1e-4, abs=1e-9)
+    assert float(lt) == float(lc) and float(nt) == float(nc)
+    assert bool((gt == gc).all())
+
+
+@pytest.mark.parametrize("N,nsteps,ck", [(32, 9, 3), (128, 5, 2)])
+def test_tape_adjoint_matches_recomputing_adjoint(N, nsteps, ck, monkeypatch):
+    """The stage-tape kernels against the recomputing adjoint (stage terms recomputed per
+    step by separate nonlinear-term and stage kernels; the path FP64 plans and the
+    shared-memory pass variants take): the same discrete gradient up to FP32 rounding."""
+    dt, nu = 2e-3, 1 / 400
+    p = _plan(N, "f32")
+    s0 = p.initial_condition("taylor_green", seed=8, pert_amp=0.05, k0=3.0)
+    lt, gt, nt = p.adjoint(s0, dt, nu, nsteps, ck)
+    monkeypatch.setenv("TG_PASS_VARIANT", "1")  # shared-memory z passes: no tape kernels
+    q = _plan(N, "f32")
+    assert q.variant == 1
+    lr, gr, nr = q.adjoint(s0, dt, nu, nsteps, ck)
+    assert float(lt) == pytest.approx(float(lr), rel=1e-6)
+    assert rel_l2(from_state(p, gt), from_state(q, gr)) < 2e-5
+    assert float(nt) == pytest.approx(float(nr), rel=1e-4)
