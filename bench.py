@@ -494,6 +494,8 @@ def run_ours(args, rank, world, local_rank):
     traffic = ncu_traffic(dom)
     roofline = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                 "traffic": traffic, "kernel": dom, "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic_source": "profiles/dram_bytes_256.txt: committed ncu capture (not measured "
+                                  "in this run); the x stage's stage-3 launch",
                 "alg_bytes_per_launch": abytes[dom]}
     step_alg = step_bytes(n)
 
