@@ -195,8 +195,10 @@ int tg_profile_passes(tg_plan* plan, void* state, double dt, double nu, double e
                       double ms[TG_PROF_SLOTS], int64_t count[TG_PROF_SLOTS]);
 
 /* Pass variant in use: bit 0 set = shared-memory z passes, bit 1 set = shared-memory x
- * passes (0: register-resident passes where they are built).  Chosen by TG_FLAG_AUTOTUNE,
- * else 0 (or the TG_PASS_VARIANT environment variable).  No reference counterpart. */
+ * passes, bit 2 set (without bit 1) = the hydro x stage with the column's spectral values
+ * stashed in shared memory between its phases (n = 64 ... 256) (0: register-resident passes
+ * where they are built).  Chosen by TG_FLAG_AUTOTUNE, else 0 (or the TG_PASS_VARIANT
+ * environment variable).  No reference counterpart. */
 int tg_pass_variant(const tg_plan* plan);
 
 /* y-pass configuration in use (0 = the default radix plan and tile width); *count (if not

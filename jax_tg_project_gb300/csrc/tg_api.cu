@@ -1065,6 +1065,7 @@ static int autotune(tg_plan* p) {
   const bool f32 = p->prec == TG_PREC_F32;
   const bool reg_z = f32 && (has_reg_adjoint(p->n) || (p->F == 3 && p->n == 96));  // z: 16 ... 256, hydro 96
   const bool reg_x = f32 && p->F == 3 && (has_reg_adjoint(p->n) || p->n == 96);  // x: hydro
+  const bool stash_x = f32 && p->F == 3 && (p->n == 64 || p->n == 96 || p->n == 128 || p->n == 256);
   const bool tune_variant = !std::getenv("TG_PASS_VARIANT");
   const bool tune_y = !std::getenv("TG_Y_CONF") && p->nyconf > 1;
   std::vector<int> cands = {0};
@@ -1072,13 +1073,15 @@ static int autotune(tg_plan* p) {
     if (reg_z) cands.push_back(1);
     if (reg_x) cands.push_back(2);
     if (reg_z && reg_x) cands.push_back(3);
+    if (stash_x) cands.push_back(4);
+    if (stash_x && reg_z) cands.push_back(5);
   }
   if (cands.size() == 1 && !tune_y) return TG_OK;
   const char* cache = std::getenv("TG_AUTOTUNE_CACHE");
   const std::string key = cache ? tune_key(p) : std::string();
   if (cache) {
     int v = -1, y = -1;
-    if (cache_lookup(cache, key, &v, &y) && v >= 0 && v <= 3 && y >= 0 && y < p->nyconf) {
+    if (cache_lookup(cache, key, &v, &y) && v >= 0 && v <= 7 && y >= 0 && y < p->nyconf) {
       if (tune_variant) p->variant = v;
       if (tune_y) p->yconf = y;
       return TG_OK;
@@ -1591,7 +1594,7 @@ struct Adjoint {
     a.spec_out = out;
     a.spec_in = X;
     a.nin = 3;
-    if (sizeof(R) == 4 && has_reg_adjoint(p->n) && p->variant == 0)
+    if (sizeof(R) == 4 && has_reg_adjoint(p->n) && (p->variant & ~4) == 0)
       return Ops<R>::go(p, OP_KX_NL_FWD, a, "kx nonlinear");
     a.flags |= FLAG_NONLIN;
     return Ops<R>::go(p, OP_KX_FWD3, a, "kx nonlinear");
@@ -1599,7 +1602,7 @@ struct Adjoint {
   // out = N'(W)^T mu = F[omega x a] + i k x F[a x u],  a = F^-1 (P mu), (u, omega) of W
   int nonlin_adj(const C* W, const C* m, C* out) {
     int rc;
-    if (sizeof(R) == 4 && has_reg_adjoint(p->n) && p->variant == 0) {
+    if (sizeof(R) == 4 && has_reg_adjoint(p->n) && (p->variant & ~4) == 0) {
       PassArgs<R> a = Ops<R>::base(p);
       a.spec_in = W;
       a.S = const_cast<C*>(m);
@@ -1796,9 +1799,9 @@ struct Adjoint {
   // The stage-tape adjoint.  seglen >= nsteps: one forward sweep records the tape of every
   // step in pinned host memory, and the backward sweep reads it back.  seglen < nsteps
   // (sqrt(n) checkpointing): a forward sweep keeps the state at the start of every segment
-  // of seglen steps (pinned host memory); the segments are then taken last to first, each
-  // recomputed from its checkpoint with its tape recorded (seglen steps of tape in host
-  // memory) and swept backwards.  While a segment is recomputed, lam (whose device buffer
+  // of seglen steps (pinned host memory) and records the last segment's tape; the segments
+  // are then taken last to first, each (but the last) recomputed from its checkpoint with its
+  // tape recorded (seglen steps of tape in host memory) and swept backwards.  While a segment is recomputed, lam (whose device buffer
   // is a tape slot then) is parked in host memory.  Device memory beyond the plan is the
   // same in both schedules: the two tape slots (eight states, the backward buffers V x 2,
   // n1, n2, n3, lam x 2, g), the working state and the partial sums.
@@ -2019,11 +2022,16 @@ struct Adjoint {
     if (nseg == 1) {  // the tape sweep is the forward run
       if ((rc = Ops<R>::start(p, cur0))) return rc;
       if ((rc = tape_forward(nsteps))) return rc;
-    } else {  // the forward run keeps the segment checkpoints
+    } else {  // the forward run keeps the segment checkpoints and records the last segment's tape
       for (int c = 0; c < nseg; ++c) {
-        TG_CUDA(cudaMemcpyAsync(hck + (size_t)c * sN, cur0, fbytes, cudaMemcpyDeviceToHost, st), "checkpoint");
+        const int len = std::min(seglen, nsteps - c * seglen);
         if ((rc = Ops<R>::start(p, cur0))) return rc;
-        if ((rc = advance(p, cur0, std::min(seglen, nsteps - c * seglen)))) return rc;
+        if (c == nseg - 1) {
+          if ((rc = tape_forward(len))) return rc;
+        } else {
+          TG_CUDA(cudaMemcpyAsync(hck + (size_t)c * sN, cur0, fbytes, cudaMemcpyDeviceToHost, st), "checkpoint");
+          if ((rc = advance(p, cur0, len))) return rc;
+        }
       }
     }
     // loss = enstrophy of the final state, lam = its gradient
@@ -2038,11 +2046,13 @@ struct Adjoint {
     } else {
       for (int c = nseg - 1; c >= 0; --c) {
         const int len = std::min(seglen, nsteps - c * seglen);
-        TG_CUDA(cudaMemcpyAsync(hlam, Lb[0], fbytes, cudaMemcpyDeviceToHost, st), "lam park");
-        TG_CUDA(cudaMemcpyAsync(cur0, hck + (size_t)c * sN, fbytes, cudaMemcpyHostToDevice, st), "checkpoint");
-        if ((rc = Ops<R>::start(p, cur0))) return rc;
-        if ((rc = tape_forward(len))) return rc;
-        TG_CUDA(cudaMemcpyAsync(Lb[0], hlam, fbytes, cudaMemcpyHostToDevice, st), "lam unpark");
+        if (c < nseg - 1) {  // recompute the segment from its checkpoint, recording its tape
+          TG_CUDA(cudaMemcpyAsync(hlam, Lb[0], fbytes, cudaMemcpyDeviceToHost, st), "lam park");
+          TG_CUDA(cudaMemcpyAsync(cur0, hck + (size_t)c * sN, fbytes, cudaMemcpyHostToDevice, st), "checkpoint");
+          if ((rc = Ops<R>::start(p, cur0))) return rc;
+          if ((rc = tape_forward(len))) return rc;
+          TG_CUDA(cudaMemcpyAsync(Lb[0], hlam, fbytes, cudaMemcpyHostToDevice, st), "lam unpark");
+        }
         if ((rc = mark(1))) return rc;
         if ((rc = backward(len))) return rc;
         if ((rc = mark(2))) return rc;
@@ -2117,7 +2127,7 @@ extern "C" int tg_adjoint(tg_plan* p, const void* state0, double dt, double nu, 
   const int sqrt_len = (int)std::ceil(std::sqrt((double)nsteps));
   const int tape_len = (checkpoint_every == TG_ADJ_HOST_TAPE) ? nsteps
                        : (checkpoint_every > 0 ? checkpoint_every : sqrt_len);
-  if (p->prec == TG_PREC_F32 && has_reg_adjoint(p->n) && p->variant == 0) {
+  if (p->prec == TG_PREC_F32 && has_reg_adjoint(p->n) && (p->variant & ~4) == 0) {
     // the stage-tape kernels: the tape of one segment (or of the whole run) in host memory
     int rc = set_coefs(p, dt, nu, 0.0);
     if (rc) return rc;

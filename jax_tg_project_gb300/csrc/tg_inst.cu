@@ -39,6 +39,11 @@ cudaError_t TG_CAT(launch, TG_REAL, TG_N)(int op, const PassArgs<TG_REAL>& a, in
                   : launch_kx_reg_adj<TG_REAL, TG_N, KX_ADJ_FWD>(a, runs, st);
     if (op == OP_KX_NL_FWD) return launch_kx_reg_adj<TG_REAL, TG_N, KX_NL_FWD>(a, runs, st);
   }
+  if constexpr (std::is_same<TG_REAL, float>::value && HasStashX<TG_N>::value) {
+    // bit 2: the x stage with the state stashed in shared memory (unless bit 1 asks for the
+    // shared-memory x pass)
+    if (reg_x && (a.variant & 4) && op == OP_KX_STAGE3) return launch_kx_stash<TG_REAL, TG_N>(a, runs, st);
+  }
   if constexpr (std::is_same<TG_REAL, float>::value && HasRegX<TG_N>::value) {
     if (reg_x) {
       if (op == OP_KX_STAGE3) return launch_kx_reg<TG_REAL, TG_N, KX_STAGE>(a, runs, st);

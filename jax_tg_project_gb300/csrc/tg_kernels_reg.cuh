@@ -597,7 +597,16 @@ struct KxRegShape {
   static constexpr int CPR = QW / 2;                // 16-byte cp.async chunks per row segment
   static constexpr int GT = QW * P;                 // threads per group
   static constexpr int TARGET = (P >= 16) ? 256 : 128;  // threads per CTA
-  static constexpr int NG = (GT >= TARGET) ? 1 : TARGET / GT;
+  static constexpr int NG0 = (GT >= TARGET) ? 1 : TARGET / GT;
+  // kz column groups of the default cutoff (K = N/3), and groups per CTA: NG0, or down to
+  // half of it when that leaves fewer idle groups in the last kz block of a row (96: 9
+  // groups, 3 per CTA instead of 4, which had transformed 48 columns for 33; 64: 6, 3)
+  static constexpr int QUADS = (N / 3 + 1 + QW - 1) / QW;
+  static constexpr int idle(int ng) { return (QUADS + ng - 1) / ng * ng - QUADS; }
+  static constexpr int best_ng(int ng, int best) {
+    return (2 * ng < NG0) ? best : best_ng(ng - 1, (idle(ng) < idle(best)) ? ng : best);
+  }
+  static constexpr int NG = best_ng(NG0, NG0);
   static constexpr int NT = NG * GT;
   // resident CTAs per SM the registers must allow (E = 12 at N = 96 needs ~168 registers)
   static constexpr int MINB = (NT >= 256) ? 2 : ((E > 8) ? 3 : 4);
@@ -885,6 +894,277 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
       inverse(std::integral_constant<int, 5>());
     }
   }
+}
+
+// ------------------------------------------------------------------ x stage, stashed state
+// The fused x stage (KX_STAGE, hydro) with the column's spectral values parked between its
+// phases in a thread-private shared-memory stash instead of in registers, so that a thread
+// holds at most one field's values (and the next field's inputs) at a time: fewer registers,
+// three CTAs (24 warps) per SM instead of two.  Each thread stashes only the mode slots it
+// owns (and only those no 2/3 cutoff removes), so the stash needs no barriers.  The state and
+// accumulator are read straight from global memory (prefetched into L2 with the next tile's
+// forward inputs while the current tile's inverse transforms run); persistent CTAs take the
+// tiles of (ky row, NG x QW kz columns, run) in kz-fastest order.
+template <int N, int P, int E> __host__ __device__ constexpr int kept_slot_count() {
+  int c = 0;
+  for (int q = 0; q < E; ++q)
+    if (!slot_cut<N, P>(q)) ++c;
+  return c;
+}
+template <int N, int P> __host__ __device__ constexpr int kept_slot_rank(int q) {
+  int c = 0;
+  for (int i = 0; i < q; ++i)
+    if (!slot_cut<N, P>(i)) ++c;
+  return c;
+}
+
+template <typename R, int N>
+struct KxStashShape {
+  using Reg = KxRegShape<R, N>;
+  using Plan = typename Reg::Plan;
+  static constexpr int P = Reg::P, E = Reg::E, QW = Reg::QW, GT = Reg::GT, NG = Reg::NG, NT = Reg::NT;
+  static constexpr int CS = Reg::CS, MMAX = Reg::MMAX;
+  static constexpr int NK = kept_slot_count<N, P, E>();  // stashed slots per field and thread
+  static constexpr int MINB = (NT >= 256) ? 3 : 5;
+  static constexpr long long stash_elems = 3LL * NK * GT;  // per group
+  static constexpr long long smem =
+      (long long)sizeof(cplx<R>) * (N + (long long)NG * QW * CS + (long long)NG * stash_elems + 2 * (MMAX + NG * QW));
+};
+// sizes with the stashed x stage (FP32)
+template <int N> struct HasStashX { static constexpr bool value = (N == 64 || N == 96 || N == 128 || N == 256); };
+
+template <typename R, int N>
+__global__ void __launch_bounds__(KxStashShape<R, N>::NT, KxStashShape<R, N>::MINB) kx_stash_kernel(const PassArgs<R> a) {
+  using C = cplx<R>;
+  using Sh = KxStashShape<R, N>;
+  using Plan = typename Sh::Plan;
+  constexpr int P = Sh::P, E = Sh::E, QW = Sh::QW, GT = Sh::GT, CS = Sh::CS, NK = Sh::NK;
+  constexpr int NBL = N / (Plan::template radix<Plan::NPASS - 1>() * P);
+  const Geo g = a.g;
+  const int K = g.K, M = g.M, Hz = g.Hz;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  const int grp = threadIdx.x / GT, lt = threadIdx.x % GT;
+  const int col = lt % QW, t = lt / QW;
+  const int kzb = ((g.Hk + QW - 1) / QW + Sh::NG - 1) / Sh::NG;  // kz blocks per ky row
+  C* xcol = tw + N + (grp * QW + col) * CS;
+  // this thread's stash: element (field f, kept slot rank qi) at st[(f * NK + qi) * GT]
+  C* st = tw + N + Sh::NG * QW * CS + grp * Sh::stash_elems + lt;
+  // integrating-factor tables (as in kx_reg_kernel), two copies by tile parity
+  C* ftab0 = tw + N + Sh::NG * QW * CS + Sh::NG * Sh::stash_elems;
+  constexpr int FT = Sh::MMAX + Sh::NG * QW;
+  auto run_fft = [&](auto& src, auto& dst, auto dir_tag) {
+    constexpr int DIR = decltype(dir_tag)::value;
+    if constexpr (GT > 32) {
+      const NamedSync ns{1 + grp, GT};
+      fft_column<Plan, DIR, Sh::Reg::PSH, false>(t, src, dst, xcol, tw, ns);
+    } else {
+      const WarpSync ws;
+      fft_column<Plan, DIR, Sh::Reg::PSH, false>(t, src, dst, xcol, tw, ws);
+    }
+  };
+  using Fwd = std::integral_constant<int, -1>;
+  using Inv = std::integral_constant<int, +1>;
+  build_twiddles<Plan>(tw, a.tw, threadIdx.x, Sh::NT);
+  const R inv_n3 = R(1) / (R(N) * R(N) * R(N));
+  const bool expl = (a.flags & FLAG_EXPLICIT) != 0;
+  const int stage = a.stage;
+
+  for (int tile = blockIdx.x, it = 0; tile < a.tiles; tile += gridDim.x, ++it) {
+    const int bkz = tile % kzb, iyc = (tile / kzb) % M, run = tile / (kzb * M);
+    const int kz0 = (bkz * Sh::NG + grp) * QW;
+    const int kz = kz0 + col;
+    const bool zok = kz < g.Hk;
+    const float kyf = float(ksigned(iyc, K)), kzf = float(kz);
+    const long long soff = (long long)run * 3 * g.sS + (long long)iyc * Hz + kz;  // + (f*M + ic)*M*Hz
+    C* ftab = ftab0 + (it & 1) * FT;
+    const C* win = a.in + (long long)run * 3 * g.sX + (long long)iyc * Hz + kz;
+    // forward inputs of field 0 (thread t reads x = t + P q into slot q)
+    C cur[E];
+#pragma unroll
+    for (int q = 0; q < E; ++q) cur[q] = zok ? win[(long long)(t + P * q) * M * Hz] : czero<C>();
+    {  // this tile's factor tables (and, on the first tile, the twiddles) before any use
+      const RunCoef cf0 = a.coef[run];
+      const R c1 = R(cf0.nu * cf0.dt), ch = R(0.5) * c1;
+      for (int i = threadIdx.x; i < M + Sh::NG * QW; i += Sh::NT) {
+        R k2;
+        if (i < M) {
+          const R kx = R(ksigned(i, K));
+          k2 = kx * kx;
+        } else {
+          const R kc = R(bkz * Sh::NG * QW + (i - M));  // kz of column i - M
+          k2 = R(kyf * kyf) + kc * kc;
+        }
+        ftab[i] = mk<C>(rexpm1<R>(-c1 * k2), rexpm1<R>(-ch * k2));
+      }
+    }
+    __syncthreads();
+    // forward transforms, field by field through one FFT body (instruction cache; the next
+    // field's inputs are loaded before the current transform), the kept slots of the result
+    // (x 1/N^3) into the stash
+#pragma unroll 1
+    for (int f = 0; f < 3; ++f) {
+      C nxt[E];
+      if (f < 2) {
+#pragma unroll
+        for (int q = 0; q < E; ++q)
+          nxt[q] = zok ? win[(f + 1) * g.sX + (long long)(t + P * q) * M * Hz] : czero<C>();
+      }
+      C* sf = st + f * NK * GT;
+      auto src = [&](int, int q) -> C { return cur[q]; };
+      auto dst = [&](int b, int r, int, C val) {
+        const int q = b + r * NBL;
+        if (!slot_cut<N, P>(q)) sf[kept_slot_rank<N, P>(q) * GT] = cscale(val, inv_n3);
+      };
+      run_fft(src, dst, Fwd());
+      if (f < 2) {
+#pragma unroll
+        for (int q = 0; q < E; ++q) cur[q] = nxt[q];
+      }
+    }
+    // Leray projection in the stash (removed modes of partly cut slots set to zero)
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      if (slot_cut<N, P>(q)) continue;
+      const int qi = kept_slot_rank<N, P>(q);
+      const int ic = kcompact_slot<N, P>(t, q, K);
+      C v0 = czero<C>(), v1 = czero<C>(), v2 = czero<C>();
+      if (zok && ic >= 0) {
+        v0 = st[(0 * NK + qi) * GT];
+        v1 = st[(1 * NK + qi) * GT];
+        v2 = st[(2 * NK + qi) * GT];
+        const float kx = float(ksigned(ic, K));
+        leray(v0, v1, v2, kx, kyf, kzf, kx * kx + kyf * kyf + kzf * kzf);
+      }
+      st[(0 * NK + qi) * GT] = v0;
+      st[(1 * NK + qi) * GT] = v1;
+      st[(2 * NK + qi) * GT] = v2;
+    }
+    // RK4 stage combine, field by field: the state / accumulator loads of all slots first
+    {
+      const RunCoef cf = a.coef[run];
+      const R h = R(cf.dt);
+      const C fyz = ftab[M + grp * QW + col];  // the (ky, kz) terms of this column
+      const C* __restrict__ Sp = a.S;
+      const C* __restrict__ Ap = a.acc;
+#pragma unroll 1
+      for (int f = 0; f < 3; ++f) {
+        C sv[NK], av[NK];
+#pragma unroll
+        for (int q = 0; q < E; ++q) {
+          if (slot_cut<N, P>(q)) continue;
+          const int qi = kept_slot_rank<N, P>(q);
+          const int ic = kcompact_slot<N, P>(t, q, K);
+          const bool ok = zok && ic >= 0;
+          const long long o = soff + ((long long)f * M + (ok ? ic : 0)) * M * Hz;
+          sv[qi] = ok ? Sp[o] : czero<C>();
+          av[qi] = (ok && stage > 1) ? Ap[o] : czero<C>();
+        }
+#pragma unroll
+        for (int q = 0; q < E; ++q) {
+          if (slot_cut<N, P>(q)) continue;
+          const int qi = kept_slot_rank<N, P>(q);
+          const int ic = kcompact_slot<N, P>(t, q, K);
+          if (!(zok && ic >= 0)) continue;  // stash entry already zero
+          const long long o = soff + ((long long)f * M + ic) * M * Hz;
+          const C n = st[(f * NK + qi) * GT];
+          const C s = sv[qi];
+          if (a.tape != nullptr) {  // adjoint tape (batch 1): n_stage for stages 1..3, V at stage 1
+            if (stage <= 3) a.tape[(long long)stage * 3 * g.sS + o] = n;
+            if (stage == 1) a.tape[o] = s;
+          }
+          C acc = av[qi];
+          C nv;
+          if (expl) {
+            const float kx = float(ksigned(ic, K));
+            const R lin = R(cf.nu * double(kx * kx + kyf * kyf + kzf * kzf));
+            const C vs = (stage > 1) ? a.vs[o] : s;
+            nv = rk4_combine<C>(stage, true, n, s, acc, vs, h, lin);
+            if (stage < 4) a.vs[o] = nv;
+          } else {
+            const C fx = ftab[ic];
+            nv = lawson_combine<C>(stage, n, s, acc, h, expm1_add(fx.x, fyz.x), expm1_add(fx.y, fyz.y));
+          }
+          if (stage < 4) a.acc[o] = acc;
+          else a.S[o] = nv;
+          st[(f * NK + qi) * GT] = nv;
+        }
+      }
+    }
+    // the next tile's forward inputs and state / accumulator rows into L2 (32-byte segments)
+    const int next = tile + gridDim.x;
+    if (next < a.tiles) {
+      const int nbkz = next % kzb, niyc = (next / kzb) % M, nrun = next / (kzb * M);
+      const int nkz0 = (nbkz * Sh::NG + grp) * QW;
+      if (nkz0 < g.Hk) {
+        const C* nw = a.in + (long long)nrun * 3 * g.sX + (long long)niyc * Hz + nkz0;
+        for (int r = lt; r < 3 * N; r += GT)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(nw + (long long)(r / N) * g.sX + (long long)(r % N) * M * Hz));
+        const long long nbase = (long long)nrun * 3 * g.sS + (long long)niyc * Hz + nkz0;
+        const int narr = (stage > 1) ? 2 : 1;
+        for (int r = lt; r < narr * 3 * M; r += GT) {
+          const C* arr = (r < 3 * M) ? a.S : a.acc;
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(arr + nbase + (long long)(r % (3 * M)) * M * Hz));
+        }
+      }
+    }
+    // inverse-x of u and curl u from the stash (one FFT body for the six fields at N >= 128)
+    C* xo = a.out + (long long)run * 6 * g.sX + (long long)iyc * Hz + kz;
+    auto values = [&](auto gi_tag, C* in) {
+      constexpr int GI = decltype(gi_tag)::value;
+#pragma unroll
+      for (int q = 0; q < E; ++q) {
+        if (slot_cut<N, P>(q)) {
+          in[q] = czero<C>();
+          continue;
+        }
+        const int qi = kept_slot_rank<N, P>(q);
+        if constexpr (GI < 3) {
+          in[q] = st[(GI * NK + qi) * GT];
+        } else {
+          const int ic = kcompact_slot<N, P>(t, q, K);
+          const float kx = float(ksigned(ic < 0 ? 0 : ic, K));
+          in[q] = curl_comp(GI - 3, st[(0 * NK + qi) * GT], st[(1 * NK + qi) * GT], st[(2 * NK + qi) * GT], kx,
+                            kyf, kzf);
+        }
+      }
+    };
+    auto inverse_of = [&](const C* in, int gi) {
+      auto src = [&](int, int q) -> C { return in[q]; };
+      C* xg = xo + gi * g.sX;
+      auto dst = [&](int, int, int x, C val) {
+        if (zok) xg[(long long)x * M * Hz] = val;
+      };
+      run_fft(src, dst, Inv());
+    };
+#pragma unroll 1
+    for (int gi = 0; gi < 6; ++gi) {
+      C in[E];
+      switch (gi) {
+        case 0: values(std::integral_constant<int, 0>(), in); break;
+        case 1: values(std::integral_constant<int, 1>(), in); break;
+        case 2: values(std::integral_constant<int, 2>(), in); break;
+        case 3: values(std::integral_constant<int, 3>(), in); break;
+        case 4: values(std::integral_constant<int, 4>(), in); break;
+        default: values(std::integral_constant<int, 5>(), in); break;
+      }
+      inverse_of(in, gi);
+    }
+  }
+}
+
+template <typename R, int N>
+static cudaError_t launch_kx_stash(const PassArgs<R>& a0, int runs, cudaStream_t st) {
+  using Sh = KxStashShape<R, N>;
+  static cudaError_t attr = set_smem(kx_stash_kernel<R, N>, Sh::smem);
+  if (attr != cudaSuccess) return attr;
+  static const int resident = resident_ctas(kx_stash_kernel<R, N>, Sh::NT, Sh::smem);
+  PassArgs<R> a = a0;
+  const int kzb = ((a.g.Hk + Sh::QW - 1) / Sh::QW + Sh::NG - 1) / Sh::NG;
+  a.tiles = kzb * a.g.M * runs;
+  const int ctas = resident > 0 ? std::min(a.tiles, resident) : a.tiles;
+  kx_stash_kernel<R, N><<<ctas, Sh::NT, Sh::smem, st>>>(a);
+  return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------ x pass, adjoint

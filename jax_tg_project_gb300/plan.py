@@ -97,7 +97,8 @@ class Plan:
 
     @property
     def variant(self):
-        """Pass variant in use: bit 0 = shared-memory z passes, bit 1 = shared-memory x passes."""
+        """Pass variant in use: bit 0 = shared-memory z passes, bit 1 = shared-memory x passes,
+        bit 2 = the x stage with its state stashed in shared memory (64 ... 256)."""
         return int(self.lib.tg_pass_variant(self._h))
 
     @property

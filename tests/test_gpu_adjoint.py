@@ -170,3 +170,20 @@ def test_tape_adjoint_matches_recomputing_adjoint(N, nsteps, ck, monkeypatch):
     assert float(lt) == pytest.approx(float(lr), rel=1e-6)
     assert rel_l2(from_state(p, gt), from_state(q, gr)) < 2e-5
     assert float(nt) == pytest.approx(float(nr), rel=1e-4)
+
+
+def test_tape_adjoint_with_stashed_x_stage(monkeypatch):
+    """The stage tape written by the stashed x stage (variant bit 2) drives the same adjoint:
+    it agrees with the tape of the register x stage to FP32 rounding."""
+    dt, nu, nsteps = 2e-3, 1 / 400, 6
+    outs = []
+    for variant in ("0", "4"):
+        monkeypatch.setenv("TG_PASS_VARIANT", variant)
+        p = _plan(128, "f32")
+        s0 = p.initial_condition("taylor_green", seed=13, pert_amp=0.05, k0=3.0)
+        loss, grad, gnu = p.adjoint(s0, dt, nu, nsteps, 3)
+        assert p.adjoint_profile()["record"] > 0.0  # the stage-tape schedule ran
+        outs.append((float(loss), from_state(p, grad), float(gnu)))
+    assert outs[1][0] == pytest.approx(outs[0][0], rel=1e-6)
+    assert rel_l2(outs[1][1], outs[0][1]) < 2e-5
+    assert outs[1][2] == pytest.approx(outs[0][2], rel=1e-4)

@@ -51,10 +51,11 @@ def oracle96():
 
 
 @pytest.mark.parametrize("variant,autotune", [("0", False), ("1", False), ("2", False), ("3", False),
-                                              (None, True)])
+                                              ("4", False), ("5", False), (None, True)])
 def test_n96_rhs_and_steps_match_oracle(oracle96, variant, autotune, monkeypatch):
     """Every pass variant at 96 (bit 0: shared-memory instead of register-resident z pass,
-    bit 1: the same for the x stage) and the autotuned plan."""
+    bit 1: the same for the x stage, bit 2: the x stage with a shared-memory stash) and the
+    autotuned plan."""
     import jax_tg_project_gb300 as tg
     if variant is None:
         monkeypatch.delenv("TG_PASS_VARIANT", raising=False)

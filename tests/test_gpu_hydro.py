@@ -115,9 +115,10 @@ def test_batched_runs_are_independent():
 def test_register_and_shared_memory_passes_agree(N, monkeypatch):
     """The register-resident x/z passes and the shared-memory passes are two
     implementations of the same step; every mix of them (TG_PASS_VARIANT bit 0: z, bit 1:
-    x) agrees with the register-resident step to FP32 round-off."""
+    x, bit 2: the x stage with a shared-memory stash, built at 64 ... 256) agrees with the
+    register-resident step to FP32 round-off."""
     steps, rhss = [], []
-    for variant in ("0", "1", "2", "3"):
+    for variant in ("0", "1", "2", "3", "4", "5"):
         monkeypatch.setenv("TG_PASS_VARIANT", variant)
         p = _plan(N, "f32")
         assert p.variant == int(variant)
@@ -126,7 +127,7 @@ def test_register_and_shared_memory_passes_agree(N, monkeypatch):
         steps.append(from_state(p, s)[0])
         r = p.rhs(p.initial_condition("taylor_green", seed=9, pert_amp=0.05, k0=3.0), nu=2e-3)
         rhss.append(from_state(p, r)[0])
-    for k in range(1, 4):
+    for k in range(1, 6):
         assert rel_l2(steps[0], steps[k]) < 2e-6, k
         assert rel_l2(rhss[0], rhss[k]) < 2e-6, k
 
@@ -141,7 +142,7 @@ def test_autotuned_plan_matches_default(N, physics, monkeypatch):
     outs = []
     for auto in (False, True):
         p = tg.Plan(N, physics=physics, precision="f32", autotune=auto)
-        assert p.variant in ((0, 1, 2, 3) if auto else (0,))
+        assert p.variant in ((0, 1, 2, 3, 4, 5) if auto else (0,))
         s = p.initial_condition(ic, seed=4, pert_amp=0.05, k0=3.0)
         p.step(s, dt=1e-3, nu=2e-3, eta=2e-3, nsteps=3)
         outs.append(from_state(p, s)[0])
@@ -273,3 +274,20 @@ def test_autotune_cache_is_written_and_read(tmp_path, monkeypatch):
     r = tg.Plan(64, batch=3, precision="f32", autotune=True)  # another key: tuned and appended
     assert len(cache.read_text().splitlines()) == 3
     del p, q, r
+
+
+@pytest.mark.parametrize("explicit", [False, True])
+def test_stashed_x_stage_matches_register_x_stage_at_256(explicit, monkeypatch):
+    """The stashed x stage (variant bit 2) and the register-resident one run the same
+    arithmetic on the 256^3 workload: three steps of a perturbed field agree to round-off,
+    for the integrating-factor and the explicit-viscosity RK4."""
+    import jax_tg_project_gb300 as tg
+    outs = []
+    for variant in ("0", "4"):
+        monkeypatch.setenv("TG_PASS_VARIANT", variant)
+        p = tg.Plan(256, precision="f32", explicit_viscosity=explicit)
+        s = p.initial_condition("taylor_green", seed=12, pert_amp=0.02, k0=4.0)
+        p.step(s, dt=2.5e-4, nu=1 / 1600, nsteps=3)
+        outs.append(from_state(p, s)[0])
+        del p, s
+    assert rel_l2(outs[0], outs[1]) < 1e-6
