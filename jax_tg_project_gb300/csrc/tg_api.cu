@@ -914,13 +914,13 @@ int dispatch(tg_plan* p, Fn&& fn) {
   return fn(Ops<float>());
 }
 
+// each coefficient given (dt > 0, nu >= 0, eta >= 0) replaces the per-run values; the others
+// keep theirs (the per-run table of tg_set_run_params)
 int set_coefs(tg_plan* p, double dt, double nu, double eta) {
-  if (dt > 0.0 || nu >= 0.0) {
-    for (auto& c : p->hcoef) {
-      if (dt > 0.0) c.dt = dt;
-      if (nu >= 0.0) c.nu = nu;
-      if (eta >= 0.0) c.eta = eta;
-    }
+  for (auto& c : p->hcoef) {
+    if (dt > 0.0) c.dt = dt;
+    if (nu >= 0.0) c.nu = nu;
+    if (eta >= 0.0) c.eta = eta;
   }
   TG_CUDA(cudaMemcpyAsync(p->coef, p->hcoef.data(), sizeof(RunCoef) * p->hcoef.size(), cudaMemcpyHostToDevice,
                           p->st),

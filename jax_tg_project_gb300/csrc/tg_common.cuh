@@ -143,6 +143,29 @@ template <typename R> struct PassArgs {
   int tiles;             // tiles of a persistent or tile-indexed kernel (set by its launcher)
 };
 
+// The geometry a kernel works with: the plan's (runtime) or, for DEFK, that of the default
+// 2/3 cutoff K = N/3 as compile-time constants, so that index and stride arithmetic and the
+// kept / removed tests of mode slots fold (the launchers pick DEFK when the plan's K is N/3).
+template <int N, bool DEFK>
+__device__ __forceinline__ Geo geo_of(const Geo& g0) {
+  if constexpr (!DEFK) {
+    return g0;
+  } else {
+    constexpr int K = N / 3, M = 2 * K + 1, Hk = K + 1, Hz = (Hk + 3) / 4 * 4;
+    Geo g;
+    g.n = N;
+    g.K = K;
+    g.M = M;
+    g.Hk = Hk;
+    g.Hz = Hz;
+    g.sS = (long long)M * M * Hz;
+    g.sX = (long long)N * M * Hz;
+    g.sY = (long long)N * N * Hz;
+    g.sP = (long long)N * N * N;
+    return g;
+  }
+}
+
 // signed wavenumber of compact index i (0..M-1)
 __device__ __forceinline__ int ksigned(int i, int K) { return i <= K ? i : i - (2 * K + 1); }
 // compact index of full-axis frequency row k, or -1 when k is dealiased away

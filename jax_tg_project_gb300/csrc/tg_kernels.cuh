@@ -295,13 +295,13 @@ kx_kernel(const PassArgs<R> a) {
 }
 
 // ------------------------------------------------------------------ y pass
-template <typename R, int N, int DIR, int YC>
+template <typename R, int N, int DIR, int YC, bool DEFK = false>
 __global__ void __launch_bounds__(YConf<N, YC>::Plan::P * YConf<N, YC>::TZ)
 ky_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Plan = typename YConf<N, YC>::Plan;
   constexpr int P = Plan::P, TZ = YConf<N, YC>::TZ, CS = ColLayout<N>::CS, NT = P * TZ;
-  const Geo g = a.g;
+  const Geo g = geo_of<N, DEFK>(a.g);
   const int K = g.K, M = g.M, Hz = g.Hz;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tw = reinterpret_cast<C*>(smem_raw);
@@ -665,6 +665,14 @@ static cudaError_t launch_ky_conf(const PassArgs<R>& a, int runs, cudaStream_t s
   static cudaError_t attr = set_smem(ky_kernel<R, N, DIR, YC>, smem);
   if (attr != cudaSuccess) return attr;
   dim3 grid((a.g.Hk + TZ - 1) / TZ, N, runs * a.nin);
+  if constexpr (sizeof(R) == 4) {  // FP32 plans: the default cutoff's geometry at compile time
+    static cudaError_t attr_d = set_smem(ky_kernel<R, N, DIR, YC, true>, smem);
+    if (attr_d != cudaSuccess) return attr_d;
+    if (a.g.K == N / 3) {
+      ky_kernel<R, N, DIR, YC, true><<<grid, NT, smem, st>>>(a);
+      return cudaGetLastError();
+    }
+  }
   ky_kernel<R, N, DIR, YC><<<grid, NT, smem, st>>>(a);
   return cudaGetLastError();
 }

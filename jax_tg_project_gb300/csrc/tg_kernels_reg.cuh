@@ -73,14 +73,14 @@ struct KzRegShape {
   static constexpr int MINB = (E > 8) ? 2 : 3;
 };
 
-template <typename R, int N>
+template <typename R, int N, bool DEFK = false>
 __global__ void __launch_bounds__(128, KzRegShape<R, N>::MINB) kz_reg_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Sh = KzRegShape<R, N>;
   using Plan = typename Sh::Plan;
   constexpr int P = Sh::P, E = Sh::E, LP = Sh::LP, CS = Sh::CS;
   constexpr int NBL = N / (Plan::template radix<Plan::NPASS - 1>() * P);
-  const Geo g = a.g;
+  const Geo g = geo_of<N, DEFK>(a.g);
   const int K = g.K, Hz = g.Hz;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tw = reinterpret_cast<C*>(smem_raw);
@@ -654,14 +654,14 @@ __device__ __forceinline__ auto uw_field(const A& v, int q, float kx, float ky, 
 // tile's inverse transforms run, the state / accumulator tiles of the CTA's next tile are
 // staged into shared memory (cp.async) and its forward inputs are prefetched into L2, so that
 // a tile starts with its operands at hand.  Otherwise one tile per CTA, ky fastest.
-template <typename R, int N, int MODE>
+template <typename R, int N, int MODE, bool DEFK = false>
 __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) kx_reg_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Sh = KxRegShape<R, N>;
   using Plan = typename Sh::Plan;
   constexpr int P = Sh::P, E = Sh::E, QW = Sh::QW, GT = Sh::GT, CS = Sh::CS;
   constexpr int NBL = N / (Plan::template radix<Plan::NPASS - 1>() * P);
-  const Geo g = a.g;
+  const Geo g = geo_of<N, DEFK>(a.g);
   const int K = g.K, M = g.M, Hz = g.Hz;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tw = reinterpret_cast<C*>(smem_raw);
@@ -933,14 +933,14 @@ struct KxStashShape {
 // sizes with the stashed x stage (FP32)
 template <int N> struct HasStashX { static constexpr bool value = (N == 64 || N == 96 || N == 128 || N == 256); };
 
-template <typename R, int N>
+template <typename R, int N, bool DEFK = false>
 __global__ void __launch_bounds__(KxStashShape<R, N>::NT, KxStashShape<R, N>::MINB) kx_stash_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Sh = KxStashShape<R, N>;
   using Plan = typename Sh::Plan;
   constexpr int P = Sh::P, E = Sh::E, QW = Sh::QW, GT = Sh::GT, CS = Sh::CS, NK = Sh::NK;
   constexpr int NBL = N / (Plan::template radix<Plan::NPASS - 1>() * P);
-  const Geo g = a.g;
+  const Geo g = geo_of<N, DEFK>(a.g);
   const int K = g.K, M = g.M, Hz = g.Hz;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tw = reinterpret_cast<C*>(smem_raw);
@@ -1158,12 +1158,15 @@ static cudaError_t launch_kx_stash(const PassArgs<R>& a0, int runs, cudaStream_t
   using Sh = KxStashShape<R, N>;
   static cudaError_t attr = set_smem(kx_stash_kernel<R, N>, Sh::smem);
   if (attr != cudaSuccess) return attr;
+  static cudaError_t attr_d = set_smem(kx_stash_kernel<R, N, true>, Sh::smem);
+  if (attr_d != cudaSuccess) return attr_d;
   static const int resident = resident_ctas(kx_stash_kernel<R, N>, Sh::NT, Sh::smem);
   PassArgs<R> a = a0;
   const int kzb = ((a.g.Hk + Sh::QW - 1) / Sh::QW + Sh::NG - 1) / Sh::NG;
   a.tiles = kzb * a.g.M * runs;
   const int ctas = resident > 0 ? std::min(a.tiles, resident) : a.tiles;
-  kx_stash_kernel<R, N><<<ctas, Sh::NT, Sh::smem, st>>>(a);
+  if (a.g.K == N / 3) kx_stash_kernel<R, N, true><<<ctas, Sh::NT, Sh::smem, st>>>(a);
+  else kx_stash_kernel<R, N><<<ctas, Sh::NT, Sh::smem, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -1645,9 +1648,12 @@ static cudaError_t launch_kz_reg(const PassArgs<R>& a, int runs, cudaStream_t st
   using Sh = KzRegShape<R, N>;
   static cudaError_t attr = set_smem(kz_reg_kernel<R, N>, Sh::smem);
   if (attr != cudaSuccess) return attr;
+  static cudaError_t attr_d = set_smem(kz_reg_kernel<R, N, true>, Sh::smem);
+  if (attr_d != cudaSuccess) return attr_d;
   const int pairs = N * N / 2;
   dim3 grid(pairs / Sh::LP, runs);
-  kz_reg_kernel<R, N><<<grid, Sh::NT, Sh::smem, st>>>(a);
+  if (a.g.K == N / 3) kz_reg_kernel<R, N, true><<<grid, Sh::NT, Sh::smem, st>>>(a);
+  else kz_reg_kernel<R, N><<<grid, Sh::NT, Sh::smem, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -1656,13 +1662,16 @@ static cudaError_t launch_kx_reg(const PassArgs<R>& a0, int runs, cudaStream_t s
   using Sh = KxRegShape<R, N>;
   static cudaError_t attr = set_smem(kx_reg_kernel<R, N, MODE>, Sh::smem);
   if (attr != cudaSuccess) return attr;
+  static cudaError_t attr_d = set_smem(kx_reg_kernel<R, N, MODE, true>, Sh::smem);
+  if (attr_d != cudaSuccess) return attr_d;
   static const int resident = resident_ctas(kx_reg_kernel<R, N, MODE>, Sh::NT, Sh::smem);
   PassArgs<R> a = a0;
   const int kzb = ((a.g.Hk + Sh::QW - 1) / Sh::QW + Sh::NG - 1) / Sh::NG;
   a.tiles = kzb * a.g.M * runs;
   int ctas = a.tiles;  // one tile per CTA
   if (MODE == KX_STAGE && Sh::PERSIST && resident > 0) ctas = std::min(a.tiles, resident);
-  kx_reg_kernel<R, N, MODE><<<ctas, Sh::NT, Sh::smem, st>>>(a);
+  if (a.g.K == N / 3) kx_reg_kernel<R, N, MODE, true><<<ctas, Sh::NT, Sh::smem, st>>>(a);
+  else kx_reg_kernel<R, N, MODE><<<ctas, Sh::NT, Sh::smem, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -91,3 +91,20 @@ def test_reduced_cutoff_keeps_taylor_green_modes(cutoff):
         assert e == pytest.approx(0.125 * math.exp(-6 * 0.01 * 0.1), rel=1e-5)
     else:
         assert e < 0.125 * math.exp(-6 * 0.01 * 0.1) * (1 + 1e-6)
+
+
+def test_each_coefficient_argument_applies_on_its_own():
+    """A call that passes only eta (dt <= 0 and nu < 0: keep the per-run dt and nu) still
+    applies eta: the MHD RHS with the table's nu and an explicit eta equals the one with both
+    given."""
+    import torch
+
+    import jax_tg_project_gb300 as tg
+    p = tg.Plan(16, physics="mhd", precision="f64")
+    s = p.initial_condition("mhd_equal_energy", seed=3, pert_amp=0.05, k0=3.0)
+    p.set_run_params(nu=0.01, eta=0.02, dt=1e-3)
+    r_only_eta = p.rhs(s, nu=-1.0, eta=0.05)
+    r_both = p.rhs(s, nu=0.01, eta=0.05)
+    r_table = p.rhs(s, nu=0.01, eta=0.02)
+    assert torch.equal(r_only_eta, r_both)
+    assert not torch.equal(r_only_eta, r_table)
