@@ -141,13 +141,13 @@ __device__ __forceinline__ C rk4_combine(int stage, bool expl, C n, C s, C& acc,
   return lawson_combine<C>(stage, n, s, acc, h, rexpm1<Re>(-lin * h), rexpm1<Re>(Re(-0.5) * lin * h));
 }
 
-template <typename R, int N, int F, int MODE>
+template <typename R, int N, int F, int MODE, bool DEFK = false>
 __global__ void __launch_bounds__(XPlanFor<N>::T::P * TileZ<R, N, F>::value, (sizeof(R) == 4) ? XPlanFor<N>::MINB : 1)
 kx_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Plan = typename XPlanFor<N>::T;
   constexpr int P = Plan::P, TZ = TileZ<R, N, F>::value, CS = ColLayout<N>::CS, NT = P * TZ;
-  const Geo g = a.g;
+  const Geo g = geo_of<N, DEFK>(a.g);
   const int K = g.K, M = g.M, Hz = g.Hz;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tw = reinterpret_cast<C*>(smem_raw);
@@ -354,7 +354,7 @@ struct KzShape {
   static constexpr long long smem = (long long)sizeof(cplx<R>) * (N + (long long)LP * BUFS * CS);
 };
 
-template <typename R, int N, int MODE>
+template <typename R, int N, int MODE, bool DEFK = false>
 __global__ void __launch_bounds__(KzShape<R, N, MODE>::P * KzShape<R, N, MODE>::LP)
 kz_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
@@ -362,7 +362,7 @@ kz_kernel(const PassArgs<R> a) {
   using Plan = typename Sh::Plan;
   constexpr int P = Sh::P, LP = Sh::LP, CS = Sh::CS, NT = P * LP, E = Plan::E;
   constexpr int RL = Plan::template radix<Plan::NPASS - 1>();
-  const Geo g = a.g;
+  const Geo g = geo_of<N, DEFK>(a.g);
   const int K = g.K, Hz = g.Hz;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tw = reinterpret_cast<C*>(smem_raw);
@@ -639,6 +639,14 @@ static cudaError_t launch_kx(const PassArgs<R>& a, int runs, cudaStream_t st) {
   static cudaError_t attr = set_smem(kx_kernel<R, N, F, MODE>, smem);
   if (attr != cudaSuccess) return attr;
   dim3 grid(a.g.M, (a.g.Hk + TZ - 1) / TZ, runs);
+  if constexpr (sizeof(R) == 4) {  // FP32 plans: the default cutoff's geometry at compile time
+    static cudaError_t attr_d = set_smem(kx_kernel<R, N, F, MODE, true>, smem);
+    if (attr_d != cudaSuccess) return attr_d;
+    if (a.g.K == N / 3) {
+      kx_kernel<R, N, F, MODE, true><<<grid, NT, smem, st>>>(a);
+      return cudaGetLastError();
+    }
+  }
   kx_kernel<R, N, F, MODE><<<grid, NT, smem, st>>>(a);
   return cudaGetLastError();  // also clears a launch-configuration error
 }
@@ -693,6 +701,14 @@ static cudaError_t launch_kz(const PassArgs<R>& a, int runs, cudaStream_t st) {
   if (attr != cudaSuccess) return attr;
   const int pairs = N * N / 2;
   dim3 grid((pairs + Sh::LP - 1) / Sh::LP, runs);
+  if constexpr (sizeof(R) == 4) {  // FP32 plans: the default cutoff's geometry at compile time
+    static cudaError_t attr_d = set_smem(kz_kernel<R, N, MODE, true>, Sh::smem);
+    if (attr_d != cudaSuccess) return attr_d;
+    if (a.g.K == N / 3) {
+      kz_kernel<R, N, MODE, true><<<grid, Sh::P * Sh::LP, Sh::smem, st>>>(a);
+      return cudaGetLastError();
+    }
+  }
   kz_kernel<R, N, MODE><<<grid, Sh::P * Sh::LP, Sh::smem, st>>>(a);
   return cudaGetLastError();
 }

@@ -243,14 +243,14 @@ struct KzRegMhdShape {
   static_assert(3 * E * P <= 6 * SS, "parked b must fit in the slots of u and b");
 };
 
-template <typename R, int N>
+template <typename R, int N, bool DEFK = false>
 __global__ void __launch_bounds__(128, 3) kz_reg_mhd_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Sh = KzRegMhdShape<R, N>;
   using Plan = typename Sh::Plan;
   constexpr int P = Sh::P, E = Sh::E, LP = Sh::LP, CS = Sh::CS;
   constexpr int NBL = N / (Plan::template radix<Plan::NPASS - 1>() * P);
-  const Geo g = a.g;
+  const Geo g = geo_of<N, DEFK>(a.g);
   const int K = g.K, Hz = g.Hz;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tw = reinterpret_cast<C*>(smem_raw);
@@ -423,9 +423,12 @@ static cudaError_t launch_kz_reg_mhd(const PassArgs<R>& a, int runs, cudaStream_
   using Sh = KzRegMhdShape<R, N>;
   static cudaError_t attr = set_smem(kz_reg_mhd_kernel<R, N>, Sh::smem);
   if (attr != cudaSuccess) return attr;
+  static cudaError_t attr_d = set_smem(kz_reg_mhd_kernel<R, N, true>, Sh::smem);
+  if (attr_d != cudaSuccess) return attr_d;
   const int pairs = N * N / 2;
   dim3 grid(pairs / Sh::LP, runs);
-  kz_reg_mhd_kernel<R, N><<<grid, Sh::NT, Sh::smem, st>>>(a);
+  if (a.g.K == N / 3) kz_reg_mhd_kernel<R, N, true><<<grid, Sh::NT, Sh::smem, st>>>(a);
+  else kz_reg_mhd_kernel<R, N><<<grid, Sh::NT, Sh::smem, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -435,14 +438,14 @@ static cudaError_t launch_kz_reg_mhd(const PassArgs<R>& a, int runs, cudaStream_
 // Order: a -> registers; each u component accumulates q, which is then transformed
 // from the registers; each omega component accumulates p in the same registers.
 // At most a, one accumulator and one transform are live: three CTAs per SM.
-template <typename R, int N>
+template <typename R, int N, bool DEFK = false>
 __global__ void __launch_bounds__(128, 3) kz_reg_adj_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Sh = KzRegMhdShape<R, N>;  // same footprint: 9 staged fields per pair
   using Plan = typename Sh::Plan;
   constexpr int P = Sh::P, E = Sh::E, LP = Sh::LP, CS = Sh::CS;
   constexpr int NBL = N / (Plan::template radix<Plan::NPASS - 1>() * P);
-  const Geo g = a.g;
+  const Geo g = geo_of<N, DEFK>(a.g);
   const int K = g.K, Hz = g.Hz;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tw = reinterpret_cast<C*>(smem_raw);
@@ -579,9 +582,12 @@ static cudaError_t launch_kz_reg_adj(const PassArgs<R>& a, int runs, cudaStream_
   using Sh = KzRegMhdShape<R, N>;
   static cudaError_t attr = set_smem(kz_reg_adj_kernel<R, N>, Sh::smem);
   if (attr != cudaSuccess) return attr;
+  static cudaError_t attr_d = set_smem(kz_reg_adj_kernel<R, N, true>, Sh::smem);
+  if (attr_d != cudaSuccess) return attr_d;
   const int pairs = N * N / 2;
   dim3 grid(pairs / Sh::LP, runs);
-  kz_reg_adj_kernel<R, N><<<grid, Sh::NT, Sh::smem, st>>>(a);
+  if (a.g.K == N / 3) kz_reg_adj_kernel<R, N, true><<<grid, Sh::NT, Sh::smem, st>>>(a);
+  else kz_reg_adj_kernel<R, N><<<grid, Sh::NT, Sh::smem, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -1184,7 +1190,7 @@ static cudaError_t launch_kx_stash(const PassArgs<R>& a0, int runs, cudaStream_t
 //                s = 4: <g4, -k^2 h E(h) V - k^2 h^2/2 E(h/2) n3>
 //                       + <L, -k^2 h E(h) V - k^2 h^2/6 (E(h) n1 + E(h/2) (n2 + n3))>
 //                s = 3: <g3, -k^2 h/2 E(h/2) V>;  s = 2: <g2, -k^2 h/2 a2>, a2 = E(h/2)(V + h/2 n1)
-template <typename R, int N, int MODE>
+template <typename R, int N, int MODE, bool DEFK = false>
 __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) kx_reg_adj_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Sh = KxRegShape<R, N>;
@@ -1194,7 +1200,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
   constexpr bool TAPE = (MODE == KX_ADJ_LOAD_T || MODE == KX_ADJ_FWD_T);
   constexpr bool HAS_FWD = (MODE == KX_ADJ_FWD || MODE == KX_ADJ_FWD_T);
   constexpr bool HAS_INV = (MODE == KX_ADJ_LOAD || MODE == KX_ADJ_LOAD_T);
-  const Geo g = a.g;
+  const Geo g = geo_of<N, DEFK>(a.g);
   const int K = g.K, M = g.M, Hz = g.Hz;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tw = reinterpret_cast<C*>(smem_raw);
@@ -1637,9 +1643,12 @@ static cudaError_t launch_kx_reg_adj(const PassArgs<R>& a, int runs, cudaStream_
   using Sh = KxRegShape<R, N>;
   static cudaError_t attr = set_smem(kx_reg_adj_kernel<R, N, MODE>, Sh::smem_adj);
   if (attr != cudaSuccess) return attr;
+  static cudaError_t attr_d = set_smem(kx_reg_adj_kernel<R, N, MODE, true>, Sh::smem_adj);
+  if (attr_d != cudaSuccess) return attr_d;
   const int quads = (a.g.Hk + Sh::QW - 1) / Sh::QW;
   dim3 grid(a.g.M, (quads + Sh::NG - 1) / Sh::NG, runs);
-  kx_reg_adj_kernel<R, N, MODE><<<grid, Sh::NT, Sh::smem_adj, st>>>(a);
+  if (a.g.K == N / 3) kx_reg_adj_kernel<R, N, MODE, true><<<grid, Sh::NT, Sh::smem_adj, st>>>(a);
+  else kx_reg_adj_kernel<R, N, MODE><<<grid, Sh::NT, Sh::smem_adj, st>>>(a);
   return cudaGetLastError();
 }
 
