@@ -13,6 +13,7 @@
 #pragma once
 
 #include <algorithm>
+#include <initializer_list>
 #include <type_traits>
 
 #include "tg_common.cuh"
@@ -620,6 +621,13 @@ enum PassOp {
   OP_KY_INV, OP_KY_FWD, OP_KZ_PROD_HD, OP_KZ_PROD_MHD, OP_KZ_C2R, OP_KZ_R2C, OP_KZ_ADJ,
   OP_KX_ADJ_LOAD, OP_KX_ADJ_FWD, OP_KX_NL_FWD, OP_COUNT  // the last three: register-resident only
 };
+
+// the first of several CUDA results that is an error, else cudaSuccess
+static inline cudaError_t first_error(std::initializer_list<cudaError_t> es) {
+  for (cudaError_t e : es)
+    if (e != cudaSuccess) return e;
+  return cudaSuccess;
+}
 
 template <typename K>
 static cudaError_t set_smem(K kernel, long long bytes) {

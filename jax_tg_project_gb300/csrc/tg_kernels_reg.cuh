@@ -660,7 +660,7 @@ __device__ __forceinline__ auto uw_field(const A& v, int q, float kx, float ky, 
 // tile's inverse transforms run, the state / accumulator tiles of the CTA's next tile are
 // staged into shared memory (cp.async) and its forward inputs are prefetched into L2, so that
 // a tile starts with its operands at hand.  Otherwise one tile per CTA, ky fastest.
-template <typename R, int N, int MODE, bool DEFK = false>
+template <typename R, int N, int MODE, bool DEFK = false, int STG = 0>
 __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) kx_reg_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Sh = KxRegShape<R, N>;
@@ -668,6 +668,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
   constexpr int P = Sh::P, E = Sh::E, QW = Sh::QW, GT = Sh::GT, CS = Sh::CS;
   constexpr int NBL = N / (Plan::template radix<Plan::NPASS - 1>() * P);
   const Geo g = geo_of<N, DEFK>(a.g);
+  const int stage = STG ? STG : a.stage;  // the RK4 stage (KX_STAGE), compile-time for STG > 0
   const int K = g.K, M = g.M, Hz = g.Hz;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tw = reinterpret_cast<C*>(smem_raw);
@@ -695,7 +696,7 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
   auto stage_state = [&](int iyc_, int bkz_, int run_) {
     const int kz0_ = (bkz_ * Sh::NG + grp) * QW;
     if (kz0_ < g.Hk) {
-      const int narr = (a.stage > 1) ? 2 : 1;
+      const int narr = (stage > 1) ? 2 : 1;
       const long long base = (long long)run_ * 3 * g.sS + (long long)iyc_ * Hz + kz0_;
       constexpr int CPR = Sh::CPR;
       const int chunks = narr * 3 * M * CPR;  // 16-byte chunks of each row segment
@@ -812,14 +813,14 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
             const long long o = soff + ((long long)f * M + ic) * M * Hz;
             const C s = stg[((long long)f * M + ic) * QW + col];
             if (a.tape != nullptr) {  // adjoint tape (batch 1): n_stage for stages 1..3, V at stage 1
-              if (a.stage <= 3) a.tape[(long long)a.stage * 3 * g.sS + o] = v[f][q];
-              if (a.stage == 1) a.tape[o] = s;
+              if (stage <= 3) a.tape[(long long)stage * 3 * g.sS + o] = v[f][q];
+              if (stage == 1) a.tape[o] = s;
             }
-            C acc = (a.stage > 1) ? stg[((long long)(3 + f) * M + ic) * QW + col] : czero<C>();
-            const C vs = (expl && a.stage > 1) ? a.vs[o] : s;
-            const C nv = expl ? rk4_combine<C>(a.stage, true, v[f][q], s, acc, vs, h, lin)
-                              : lawson_combine<C>(a.stage, v[f][q], s, acc, h, m1, mh);
-            if (a.stage < 4) {
+            C acc = (stage > 1) ? stg[((long long)(3 + f) * M + ic) * QW + col] : czero<C>();
+            const C vs = (expl && stage > 1) ? a.vs[o] : s;
+            const C nv = expl ? rk4_combine<C>(stage, true, v[f][q], s, acc, vs, h, lin)
+                              : lawson_combine<C>(stage, v[f][q], s, acc, h, m1, mh);
+            if (stage < 4) {
               a.acc[o] = acc;
               if (expl) a.vs[o] = nv;
             } else {
@@ -939,7 +940,7 @@ struct KxStashShape {
 // sizes with the stashed x stage (FP32)
 template <int N> struct HasStashX { static constexpr bool value = (N == 64 || N == 96 || N == 128 || N == 256); };
 
-template <typename R, int N, bool DEFK = false>
+template <typename R, int N, bool DEFK = false, int STG = 0>
 __global__ void __launch_bounds__(KxStashShape<R, N>::NT, KxStashShape<R, N>::MINB) kx_stash_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Sh = KxStashShape<R, N>;
@@ -974,7 +975,7 @@ __global__ void __launch_bounds__(KxStashShape<R, N>::NT, KxStashShape<R, N>::MI
   build_twiddles<Plan>(tw, a.tw, threadIdx.x, Sh::NT);
   const R inv_n3 = R(1) / (R(N) * R(N) * R(N));
   const bool expl = (a.flags & FLAG_EXPLICIT) != 0;
-  const int stage = a.stage;
+  const int stage = STG ? STG : a.stage;  // compile-time for STG > 0
 
   for (int tile = blockIdx.x, it = 0; tile < a.tiles; tile += gridDim.x, ++it) {
     const int bkz = tile % kzb, iyc = (tile / kzb) % M, run = tile / (kzb * M);
@@ -1164,15 +1165,26 @@ static cudaError_t launch_kx_stash(const PassArgs<R>& a0, int runs, cudaStream_t
   using Sh = KxStashShape<R, N>;
   static cudaError_t attr = set_smem(kx_stash_kernel<R, N>, Sh::smem);
   if (attr != cudaSuccess) return attr;
-  static cudaError_t attr_d = set_smem(kx_stash_kernel<R, N, true>, Sh::smem);
+  static cudaError_t attr_d = first_error({set_smem(kx_stash_kernel<R, N, true, 1>, Sh::smem),
+                                           set_smem(kx_stash_kernel<R, N, true, 2>, Sh::smem),
+                                           set_smem(kx_stash_kernel<R, N, true, 3>, Sh::smem),
+                                           set_smem(kx_stash_kernel<R, N, true, 4>, Sh::smem)});
   if (attr_d != cudaSuccess) return attr_d;
   static const int resident = resident_ctas(kx_stash_kernel<R, N>, Sh::NT, Sh::smem);
   PassArgs<R> a = a0;
   const int kzb = ((a.g.Hk + Sh::QW - 1) / Sh::QW + Sh::NG - 1) / Sh::NG;
   a.tiles = kzb * a.g.M * runs;
   const int ctas = resident > 0 ? std::min(a.tiles, resident) : a.tiles;
-  if (a.g.K == N / 3) kx_stash_kernel<R, N, true><<<ctas, Sh::NT, Sh::smem, st>>>(a);
-  else kx_stash_kernel<R, N><<<ctas, Sh::NT, Sh::smem, st>>>(a);
+  if (a.g.K == N / 3) {  // default cutoff: geometry and RK4 stage at compile time
+    switch (a.stage) {
+      case 1: kx_stash_kernel<R, N, true, 1><<<ctas, Sh::NT, Sh::smem, st>>>(a); break;
+      case 2: kx_stash_kernel<R, N, true, 2><<<ctas, Sh::NT, Sh::smem, st>>>(a); break;
+      case 3: kx_stash_kernel<R, N, true, 3><<<ctas, Sh::NT, Sh::smem, st>>>(a); break;
+      default: kx_stash_kernel<R, N, true, 4><<<ctas, Sh::NT, Sh::smem, st>>>(a); break;
+    }
+  } else {
+    kx_stash_kernel<R, N><<<ctas, Sh::NT, Sh::smem, st>>>(a);
+  }
   return cudaGetLastError();
 }
 
@@ -1673,14 +1685,31 @@ static cudaError_t launch_kx_reg(const PassArgs<R>& a0, int runs, cudaStream_t s
   if (attr != cudaSuccess) return attr;
   static cudaError_t attr_d = set_smem(kx_reg_kernel<R, N, MODE, true>, Sh::smem);
   if (attr_d != cudaSuccess) return attr_d;
+  if constexpr (MODE == KX_STAGE) {
+    static cudaError_t attr_s = first_error({set_smem(kx_reg_kernel<R, N, MODE, true, 1>, Sh::smem),
+                                             set_smem(kx_reg_kernel<R, N, MODE, true, 2>, Sh::smem),
+                                             set_smem(kx_reg_kernel<R, N, MODE, true, 3>, Sh::smem),
+                                             set_smem(kx_reg_kernel<R, N, MODE, true, 4>, Sh::smem)});
+    if (attr_s != cudaSuccess) return attr_s;
+  }
   static const int resident = resident_ctas(kx_reg_kernel<R, N, MODE>, Sh::NT, Sh::smem);
   PassArgs<R> a = a0;
   const int kzb = ((a.g.Hk + Sh::QW - 1) / Sh::QW + Sh::NG - 1) / Sh::NG;
   a.tiles = kzb * a.g.M * runs;
   int ctas = a.tiles;  // one tile per CTA
   if (MODE == KX_STAGE && Sh::PERSIST && resident > 0) ctas = std::min(a.tiles, resident);
-  if (a.g.K == N / 3) kx_reg_kernel<R, N, MODE, true><<<ctas, Sh::NT, Sh::smem, st>>>(a);
-  else kx_reg_kernel<R, N, MODE><<<ctas, Sh::NT, Sh::smem, st>>>(a);
+  if (MODE == KX_STAGE && a.g.K == N / 3) {  // default cutoff: geometry and RK4 stage at compile time
+    switch (a.stage) {
+      case 1: kx_reg_kernel<R, N, MODE, true, 1><<<ctas, Sh::NT, Sh::smem, st>>>(a); break;
+      case 2: kx_reg_kernel<R, N, MODE, true, 2><<<ctas, Sh::NT, Sh::smem, st>>>(a); break;
+      case 3: kx_reg_kernel<R, N, MODE, true, 3><<<ctas, Sh::NT, Sh::smem, st>>>(a); break;
+      default: kx_reg_kernel<R, N, MODE, true, 4><<<ctas, Sh::NT, Sh::smem, st>>>(a); break;
+    }
+  } else if (a.g.K == N / 3) {
+    kx_reg_kernel<R, N, MODE, true><<<ctas, Sh::NT, Sh::smem, st>>>(a);
+  } else {
+    kx_reg_kernel<R, N, MODE><<<ctas, Sh::NT, Sh::smem, st>>>(a);
+  }
   return cudaGetLastError();
 }
 
