@@ -17,9 +17,9 @@
 // Shared memory holds only the twiddle table and one exchange column per
 // transform, so barriers are per warp (z) or per 4-column group (x, a named
 // barrier), never CTA-wide inside the loops.  The z passes at N >= 128 use the
-// XOR-swizzled exchange layout (no bank conflicts) and form the twiddle powers in
-// registers from one table read per butterfly; the x pass keeps the table (its
-// four columns share each twiddle, so a read is a broadcast).
+// XOR-swizzled exchange layout (no bank conflicts); the x and z passes form the twiddle
+// powers in registers from one table read per butterfly (the x pass, whose four columns share
+// each read, waits on the shared-memory queue more than on its arithmetic).
 #pragma once
 
 #include <algorithm>
@@ -722,10 +722,10 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
     constexpr int DIR = decltype(dir_tag)::value;
     if constexpr (GT > 32) {
       const NamedSync ns{1 + grp, GT};
-      fft_column<Plan, DIR, Sh::PSH, false>(t, src, dst, xcol, tw, ns);
+      fft_column<Plan, DIR, Sh::PSH, true>(t, src, dst, xcol, tw, ns);
     } else {
       const WarpSync ws;
-      fft_column<Plan, DIR, Sh::PSH, false>(t, src, dst, xcol, tw, ws);
+      fft_column<Plan, DIR, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
     }
   };
   auto gsync = [&]() {
