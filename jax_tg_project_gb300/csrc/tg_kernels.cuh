@@ -326,7 +326,7 @@ ky_kernel(const PassArgs<R> a) {
     auto dst = [&](int, int, int y, C v) {
       if (zok) out[(long long)y * Hz] = v;
     };
-    fft_column<Plan, +1>(t, src, dst, xcol, tw);
+    fft_column<Plan, +1, 4, true>(t, src, dst, xcol, tw);  // twiddle powers in registers
   } else {
     const C* in = a.in + ((long long)run * a.nin + f) * g.sY + (long long)x * N * Hz + kz;
     C* out = a.out + ((long long)run * a.nin + f) * g.sX + (long long)x * M * Hz + kz;
@@ -336,7 +336,7 @@ ky_kernel(const PassArgs<R> a) {
       const int ic = kcompact(k, N, K);
       if (zok && ic >= 0) out[(long long)ic * Hz] = v;
     };
-    fft_column<Plan, -1>(t, src, dst, xcol, tw);
+    fft_column<Plan, -1, 4, true>(t, src, dst, xcol, tw);
   }
 }
 
