@@ -67,6 +67,16 @@ template <> __device__ __forceinline__ float2 cscale<float2>(float2 a, float s) 
   asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(make_float2(s, s))));
   return unpack2(r);
 }
+// lane-wise a * b + c (one rounding per lane) and -a (exact): the two lines of a packed pair
+template <typename C> __device__ __forceinline__ C lane_fma(C a, C b, C c) {
+  return mk<C>(a.x * b.x + c.x, a.y * b.y + c.y);
+}
+template <> __device__ __forceinline__ float2 lane_fma<float2>(float2 a, float2 b, float2 c) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)), "l"(pack2(c)));
+  return unpack2(r);
+}
+template <typename C> __device__ __forceinline__ C lane_neg(C a) { return cscale(a, decltype(C::x)(-1)); }
 template <typename C> __device__ __forceinline__ C cconj(C a) { return mk<C>(a.x, -a.y); }
 // multiply by i*s (s = +1 or -1 at compile time, or any real)
 template <typename C> __device__ __forceinline__ C cmul_i(C a) { return mk<C>(-a.y, a.x); }
@@ -242,14 +252,51 @@ struct NamedSync {  // bar.sync on a named barrier shared by `count` threads (wh
 // Thread t reads exactly the inputs n = t (mod P) in pass 0 and holds exactly the
 // outputs k = t (mod P) after the last pass (q = b + r*N/(R*P) in both), so a
 // transform can take its input from, and leave its output in, registers.
-template <class Plan, int DIR, int I, int NS, int PSH = 4, bool TWC = false, typename C, class Src, class Dst,
-          class Sync = CtaSync>
+// Twiddles held in registers (TWR): one thread's factors W_{NS R}^{jm r} of every pass after
+// the first, read once from the per-pass tables and kept across all transforms the thread runs.
+// Pass I occupies entries twr_offset<Plan, I>() + r - 1 (1 <= r < R); jm = t mod NS is the same
+// for all butterflies of a thread when P is a multiple of NS (checked).
+template <class Plan, int I>
+__host__ __device__ constexpr int twr_offset() {
+  if constexpr (I <= 1) return 0;
+  else return twr_offset<Plan, I - 1>() + Plan::template radix<I - 1>() - 1;
+}
+template <class Plan> struct TwrCount {
+  static constexpr int value = twr_offset<Plan, Plan::NPASS>();
+};
+template <class Plan, int I = 1, int NS = Plan::template radix<0>()>
+__host__ __device__ constexpr bool twr_ok() {
+  if constexpr (I >= Plan::NPASS) return true;
+  else return (Plan::P % NS == 0) && twr_ok<Plan, I + 1, NS * Plan::template radix<I>()>();
+}
+template <class Plan, int I = 1, int NS = Plan::template radix<0>(), typename C>
+__device__ __forceinline__ void load_twiddle_regs(C* wr, const C* tw, int t) {
+  if constexpr (I < Plan::NPASS) {
+    constexpr int R = Plan::template radix<I>();
+    static_assert(Plan::P % NS == 0, "register twiddles need P to be a multiple of every pass's NS");
+    constexpr int OFF = NS - Plan::template radix<0>();
+    constexpr int OR = twr_offset<Plan, I>();
+    const int jm = jmod<NS>(t);
+#pragma unroll
+    for (int r = 1; r < R; ++r) wr[OR + r - 1] = tw[OFF + (r - 1) * NS + jm];
+    load_twiddle_regs<Plan, I + 1, NS * R>(wr, tw, t);
+  }
+}
+
+template <class Plan, int DIR, int I, int NS, int PSH = 4, bool TWC = false, bool TWR = false, int XOFF = 0,
+          bool FRESH = false, typename C, class Src, class Dst, class Sync = CtaSync>
 __device__ __forceinline__ void fft_pass(int t, Src& src, Dst& dst, C* xb, const C* tw,
-                                         const Sync& sync = Sync()) {
+                                         const Sync& sync = Sync(), const C* wr = nullptr) {
   constexpr int N = Plan::N, P = Plan::P;
   constexpr int R = Plan::template radix<I>();
   constexpr int NB = N / (R * P);
   constexpr bool LAST = (I == Plan::NPASS - 1);
+  // XOFF > 0: two exchange columns XOFF apart, pass I writing column I % 2.  With three passes
+  // every transform writes the first, then the second, so a write to a column always follows a
+  // barrier that every thread passed after its reads of that column: one barrier per exchange
+  static_assert(XOFF == 0 || Plan::NPASS == 3, "double exchange columns need three passes");
+  constexpr int ROFF = (XOFF > 0 && I > 0 && ((I - 1) & 1)) ? XOFF : 0;  // column read by pass I
+  constexpr int WOFF = (XOFF > 0 && (I & 1)) ? XOFF : 0;                 // column written by pass I
   C v[NB][R];
 #pragma unroll
   for (int b = 0; b < NB; ++b) {
@@ -259,14 +306,18 @@ __device__ __forceinline__ void fft_pass(int t, Src& src, Dst& dst, C* xb, const
       if constexpr (I == 0) {
         v[b][r] = src(j + r * (N / R), b + r * NB);
       } else {
-        v[b][r] = xb[padx<PSH>(j + r * (N / R))];
+        v[b][r] = xb[ROFF + padx<PSH>(j + r * (N / R))];
       }
     }
     if constexpr (I > 0) {
       const int jm = jmod<NS>(j);
       constexpr int OFF = NS - Plan::template radix<0>();
       C w[R];
-      if constexpr (TWC && sizeof(w[0].x) == 4) {
+      if constexpr (TWR) {
+        constexpr int OR = twr_offset<Plan, I>();
+#pragma unroll
+        for (int r = 1; r < R; ++r) w[r] = wr[OR + r - 1];
+      } else if constexpr (TWC && sizeof(w[0].x) == 4) {
         // read W^jm only and form W^(jm r) = W^(jm r/2) W^(jm (r - r/2)) in registers
         // (at most log2(R) products deep): fewer table reads on the shared-memory pipe
         w[1] = tw[OFF + jm];
@@ -281,22 +332,24 @@ __device__ __forceinline__ void fft_pass(int t, Src& src, Dst& dst, C* xb, const
         }
       }
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], w[r]);
+      for (int r = 1; r < R; ++r) v[b][r] = (TWR && DIR > 0) ? cmulc(v[b][r], w[r]) : cmul(v[b][r], w[r]);
     }
     dft<R, DIR>(v[b]);
   }
   if constexpr (!LAST) {
-    sync();  // every reader of xb (this or a previous transform) is done
+    // every reader of xb (this or a previous transform) is done; FRESH: the column's only
+    // transform, whose first exchange follows a barrier already (nobody has read xb yet)
+    if constexpr (XOFF == 0 && !(FRESH && I == 0)) sync();
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
       const int j = t + P * b;
       const int jm = jmod<NS>(j);
       const int base = (j - jm) * R + jm;
 #pragma unroll
-      for (int r = 0; r < R; ++r) xb[padx<PSH>(base + r * NS)] = v[b][r];
+      for (int r = 0; r < R; ++r) xb[WOFF + padx<PSH>(base + r * NS)] = v[b][r];
     }
     sync();
-    fft_pass<Plan, DIR, I + 1, NS * R, PSH, TWC>(t, src, dst, xb, tw, sync);
+    fft_pass<Plan, DIR, I + 1, NS * R, PSH, TWC, TWR, XOFF>(t, src, dst, xb, tw, sync, wr);
   } else {
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
@@ -307,10 +360,17 @@ __device__ __forceinline__ void fft_pass(int t, Src& src, Dst& dst, C* xb, const
   }
 }
 
-template <class Plan, int DIR, int PSH = 4, bool TWC = false, typename C, class Src, class Dst, class Sync = CtaSync>
+template <class Plan, int DIR, int PSH = 4, bool TWC = false, int XOFF = 0, bool FRESH = false, typename C,
+          class Src, class Dst, class Sync = CtaSync>
 __device__ __forceinline__ void fft_column(int t, Src& src, Dst& dst, C* xb, const C* tw,
                                            const Sync& sync = Sync()) {
-  fft_pass<Plan, DIR, 0, 1, PSH, TWC>(t, src, dst, xb, tw, sync);
+  fft_pass<Plan, DIR, 0, 1, PSH, TWC, false, XOFF, FRESH>(t, src, dst, xb, tw, sync);
+}
+
+// the same with the twiddles of every pass in registers (load_twiddle_regs)
+template <class Plan, int DIR, int PSH = 4, typename C, class Src, class Dst, class Sync>
+__device__ __forceinline__ void fft_column_wr(int t, Src& src, Dst& dst, C* xb, const C* wr, const Sync& sync) {
+  fft_pass<Plan, DIR, 0, 1, PSH, false, true>(t, src, dst, xb, wr, sync, wr);
 }
 
 // register slot q of the output (b, r) of the last pass

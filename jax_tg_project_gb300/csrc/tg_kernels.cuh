@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(YConf<N, YC>::Plan::P * YConf<N, YC>::TZ)
 ky_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
   using Plan = typename YConf<N, YC>::Plan;
-  constexpr int P = Plan::P, TZ = YConf<N, YC>::TZ, CS = ColLayout<N>::CS, NT = P * TZ;
+  constexpr int P = Plan::P, TZ = YConf<N, YC>::TZ, CS = ColLayout<N>::CS, NT = P * TZ, E = Plan::E;
   const Geo g = geo_of<N, DEFK>(a.g);
   const int K = g.K, M = g.M, Hz = g.Hz;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -312,31 +312,39 @@ ky_kernel(const PassArgs<R> a) {
   const int f = blockIdx.z % a.nin, run = blockIdx.z / a.nin;
   const int kz = z0 + col;
   const bool zok = kz < g.Hk;
-  build_twiddles<Plan>(tw, a.tw, threadIdx.x, NT);
-  __syncthreads();
   C* xcol = xb + col * CS;
+  // the column's inputs (first pass of thread t: index t + P q into slot q) are loaded before
+  // the twiddle table is built, so that the two global round trips overlap
+  C pre[E];
   if constexpr (DIR > 0) {
     const C* in = a.in + ((long long)run * a.nin + f) * g.sX + (long long)x * M * Hz + kz;
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+      const int ic = slot_cut<N, P>(q) ? -1 : kcompact(t + P * q, N, K);  // always-removed rows
+      pre[q] = (zok && ic >= 0) ? in[(long long)ic * Hz] : czero<C>();
+    }
+  } else {
+    const C* in = a.in + ((long long)run * a.nin + f) * g.sY + (long long)x * N * Hz + kz;
+#pragma unroll
+    for (int q = 0; q < E; ++q) pre[q] = zok ? in[(long long)(t + P * q) * Hz] : czero<C>();
+  }
+  build_twiddles<Plan>(tw, a.tw, threadIdx.x, NT);
+  __syncthreads();
+  auto src = [&](int, int q) -> C { return pre[q]; };
+  if constexpr (DIR > 0) {
     C* out = a.out + ((long long)run * a.nin + f) * g.sY + (long long)x * N * Hz + kz;
-    auto src = [&](int k, int q) -> C {
-      if (slot_cut<N, P>(q)) return czero<C>();  // always-removed rows
-      const int ic = kcompact(k, N, K);
-      return (zok && ic >= 0) ? in[(long long)ic * Hz] : czero<C>();
-    };
     auto dst = [&](int, int, int y, C v) {
       if (zok) out[(long long)y * Hz] = v;
     };
-    fft_column<Plan, +1, 4, true>(t, src, dst, xcol, tw);  // twiddle powers in registers
+    fft_column<Plan, +1, 4, true, 0, true>(t, src, dst, xcol, tw);  // twiddle powers in registers
   } else {
-    const C* in = a.in + ((long long)run * a.nin + f) * g.sY + (long long)x * N * Hz + kz;
     C* out = a.out + ((long long)run * a.nin + f) * g.sX + (long long)x * M * Hz + kz;
-    auto src = [&](int y, int) -> C { return zok ? in[(long long)y * Hz] : czero<C>(); };
     auto dst = [&](int b, int r, int k, C v) {
       if (slot_cut<N, P>(out_slot<Plan>(b, r))) return;  // always-removed rows
       const int ic = kcompact(k, N, K);
       if (zok && ic >= 0) out[(long long)ic * Hz] = v;
     };
-    fft_column<Plan, -1, 4, true>(t, src, dst, xcol, tw);
+    fft_column<Plan, -1, 4, true, 0, true>(t, src, dst, xcol, tw);
   }
 }
 

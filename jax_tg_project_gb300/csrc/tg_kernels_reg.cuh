@@ -107,6 +107,16 @@ __global__ void __launch_bounds__(128, KzRegShape<R, N>::MINB) kz_reg_kernel(con
   build_twiddles<Plan>(tw, a.tw, threadIdx.x, Sh::NT);
   __syncthreads();
   const WarpSync ws;
+  // this thread's twiddles of passes 1.. in registers, shared by the nine transforms (where
+  // every pass's butterflies of a thread share them), else formed per pass from the table
+  constexpr bool TWR = twr_ok<Plan>();
+  C wr[TWR ? TwrCount<Plan>::value : 1];
+  if constexpr (TWR) load_twiddle_regs<Plan>(wr, tw, t);
+  auto fftz = [&](auto& src, auto& dst, auto dir_tag) {
+    constexpr int DIR = decltype(dir_tag)::value;
+    if constexpr (TWR) fft_column_wr<Plan, DIR, Sh::PSH>(t, src, dst, xcol, wr, ws);
+    else fft_column<Plan, DIR, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
+  };
 
   // Z = A + iB for rows (x, y0), (x, y0+1); kz > K is zero, kz < 0 by Hermitian symmetry
   auto packed = [&](const C* fld) {
@@ -137,7 +147,7 @@ __global__ void __launch_bounds__(128, KzRegShape<R, N>::MINB) kz_reg_kernel(con
     __syncwarp();
     auto src = packed(stg + f * 2 * Hz);
     auto dst = [&](int b, int r, int, C v) { z[b + r * NBL] = v; };
-    fft_column<Plan, +1, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
+    fftz(src, dst, std::integral_constant<int, +1>());
   };
   auto inv_u = [&](auto c_tag) {
     constexpr int c = decltype(c_tag)::value;
@@ -159,8 +169,8 @@ __global__ void __launch_bounds__(128, KzRegShape<R, N>::MINB) kz_reg_kernel(con
     constexpr int c1 = (w + 1) % 3, c2 = (w + 2) % 3;
 #pragma unroll
     for (int q = 0; q < E; ++q) {
-      m[c1][q] = mk<C>(m[c1][q].x + u[c2][q].x * z[q].x, m[c1][q].y + u[c2][q].y * z[q].y);
-      m[c2][q] = mk<C>(m[c2][q].x - u[c1][q].x * z[q].x, m[c2][q].y - u[c1][q].y * z[q].y);
+      m[c1][q] = lane_fma(u[c2][q], z[q], m[c1][q]);
+      m[c2][q] = lane_fma(u[c1][q], lane_neg(z[q]), m[c2][q]);
     }
   };
 #pragma unroll 1
@@ -194,7 +204,7 @@ __global__ void __launch_bounds__(128, KzRegShape<R, N>::MINB) kz_reg_kernel(con
     }
     auto src = [&](int, int q) -> C { return in[q]; };
     auto dst = [&](int b, int r, int, C v) { z[b + r * NBL] = v; };
-    fft_column<Plan, -1, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
+    fftz(src, dst, std::integral_constant<int, -1>());
     // partner value Z(N-k) for k = t + P q: lane (P-t) mod P, slot E-1-q (t != 0) or
     // this lane, slot (E-q) mod E (t == 0)
     C zm[E];
@@ -382,8 +392,8 @@ __global__ void __launch_bounds__(128, 3) kz_reg_mhd_kernel(const PassArgs<R> a)
     constexpr int c1 = (w + 1) % 3, c2 = (w + 2) % 3;
 #pragma unroll
     for (int q = 0; q < E; ++q) {
-      m[c1][q] = mk<C>(m[c1][q].x + u[c2][q].x * z[q].x, m[c1][q].y + u[c2][q].y * z[q].y);
-      m[c2][q] = mk<C>(m[c2][q].x - u[c1][q].x * z[q].x, m[c2][q].y - u[c1][q].y * z[q].y);
+      m[c1][q] = lane_fma(u[c2][q], z[q], m[c1][q]);
+      m[c2][q] = lane_fma(u[c1][q], lane_neg(z[q]), m[c2][q]);
     }
   };
   add_uw(I0(), std::integral_constant<int, 2>());
@@ -623,6 +633,12 @@ struct KxRegShape {
   static constexpr int PSH = 3;
   // exchange column stride: = 4 (mod 16) for 4-column groups, = 2 for 8 (bank-conflict model)
   static constexpr int CS = ColLayout<N, PSH, (QW == 8) ? 2 : 4>::CS;
+  // at 96 the register x stage alternates between two exchange columns per kz column (one group
+  // barrier per exchange instead of two; batched 96^3 x stage 173.5 -> 161.4 us).  At 128 and 256
+  // the larger shared-memory footprint measured slower (20.9 -> 22.3 and 122.0 -> 136.2 us).
+  // XOFF is the distance between the two columns
+  static constexpr int XCOLS = (Plan::NPASS == 3 && N == 96) ? 2 : 1;
+  static constexpr int XOFF = (XCOLS == 2) ? NG * QW * CS : 0;
   static constexpr int MMAX = 2 * (N / 3) + 1;
   // per group: state and accumulator tiles [2][3][M][QW], staged by cp.async
   static constexpr long long stage_elems = 2LL * 3 * MMAX * QW;
@@ -631,7 +647,7 @@ struct KxRegShape {
   // (two copies of the factor tables: the persistent x stage writes a tile's while the previous
   // tile's may still be read)
   static constexpr long long smem =
-      (long long)sizeof(cplx<R>) * (N + (long long)NG * QW * CS + (long long)NG * stage_elems + 2 * (MMAX + NG * QW));
+      (long long)sizeof(cplx<R>) * (N + (long long)XCOLS * NG * QW * CS + (long long)NG * stage_elems + 2 * (MMAX + NG * QW));
   // adjoint kernels, per group: a ring of four [N][QW] input tiles of the forward transforms,
   // or up to two [3][M][QW] spectral tiles, both staged by cp.async
   static constexpr long long ring_elems = 4LL * N * QW;
@@ -681,14 +697,14 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
   auto tile_iyc = [&](int tl) { return KZF ? (tl / kzb) % M : tl % M; };
   C* xcol = tw + N + (grp * QW + col) * CS;
   // [0] state, [1] accumulator: [3][M][QW] each
-  C* stg = tw + N + Sh::NG * QW * CS + grp * Sh::stage_elems;
+  C* stg = tw + N + Sh::XCOLS * Sh::NG * QW * CS + grp * Sh::stage_elems;
   // integrating factors of the Lawson stages: expm1(-c (kx^2 + q)) with c = nu h (or nu h / 2)
   // and q = ky^2 + kz^2 is expm1(a) + expm1(b) + expm1(a) expm1(b), a = -c kx^2, b = -c q, an
   // exact identity; the kx terms (M entries) and the (ky, kz) terms of the tile's columns are
   // tabulated per tile, so that no mode evaluates expm1 (the factors stay in delta form).
   // Two copies, by tile parity: a tile's table is written while the previous tile's may
   // still be read
-  C* ftab0 = tw + N + Sh::NG * QW * CS + Sh::NG * Sh::stage_elems;
+  C* ftab0 = tw + N + Sh::XCOLS * Sh::NG * QW * CS + Sh::NG * Sh::stage_elems;
   constexpr int FT = Sh::MMAX + Sh::NG * QW;
   // stage the state (and accumulator) tiles of this group's columns of tile (iyc, bkz, run):
   // rows of QW consecutive kz are 32-byte aligned (Hz % 4 == 0, kz0 a multiple of QW); chunks
@@ -722,10 +738,10 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
     constexpr int DIR = decltype(dir_tag)::value;
     if constexpr (GT > 32) {
       const NamedSync ns{1 + grp, GT};
-      fft_column<Plan, DIR, Sh::PSH, true>(t, src, dst, xcol, tw, ns);
+      fft_column<Plan, DIR, Sh::PSH, true, Sh::XOFF>(t, src, dst, xcol, tw, ns);
     } else {
       const WarpSync ws;
-      fft_column<Plan, DIR, Sh::PSH, true>(t, src, dst, xcol, tw, ws);
+      fft_column<Plan, DIR, Sh::PSH, true, Sh::XOFF>(t, src, dst, xcol, tw, ws);
     }
   };
   auto gsync = [&]() {
