@@ -648,6 +648,9 @@ struct KxRegShape {
   // tile's may still be read)
   static constexpr long long smem =
       (long long)sizeof(cplx<R>) * (N + (long long)XCOLS * NG * QW * CS + (long long)NG * stage_elems + 2 * (MMAX + NG * QW));
+  // RK4 stage 1 stages the state only (no accumulator yet): its kernel lays out and requests
+  // half the staging area
+  static constexpr long long smem1 = smem - (long long)sizeof(cplx<R>) * NG * (stage_elems / 2);
   // adjoint kernels, per group: a ring of four [N][QW] input tiles of the forward transforms,
   // or up to two [3][M][QW] spectral tiles, both staged by cp.async
   static constexpr long long ring_elems = 4LL * N * QW;
@@ -697,14 +700,15 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
   auto tile_iyc = [&](int tl) { return KZF ? (tl / kzb) % M : tl % M; };
   C* xcol = tw + N + (grp * QW + col) * CS;
   // [0] state, [1] accumulator: [3][M][QW] each
-  C* stg = tw + N + Sh::XCOLS * Sh::NG * QW * CS + grp * Sh::stage_elems;
+  constexpr long long SE = (STG == 1) ? Sh::stage_elems / 2 : Sh::stage_elems;  // staging area per group
+  C* stg = tw + N + Sh::XCOLS * Sh::NG * QW * CS + grp * SE;
   // integrating factors of the Lawson stages: expm1(-c (kx^2 + q)) with c = nu h (or nu h / 2)
   // and q = ky^2 + kz^2 is expm1(a) + expm1(b) + expm1(a) expm1(b), a = -c kx^2, b = -c q, an
   // exact identity; the kx terms (M entries) and the (ky, kz) terms of the tile's columns are
   // tabulated per tile, so that no mode evaluates expm1 (the factors stay in delta form).
   // Two copies, by tile parity: a tile's table is written while the previous tile's may
   // still be read
-  C* ftab0 = tw + N + Sh::XCOLS * Sh::NG * QW * CS + Sh::NG * Sh::stage_elems;
+  C* ftab0 = tw + N + Sh::XCOLS * Sh::NG * QW * CS + Sh::NG * SE;
   constexpr int FT = Sh::MMAX + Sh::NG * QW;
   // stage the state (and accumulator) tiles of this group's columns of tile (iyc, bkz, run):
   // rows of QW consecutive kz are 32-byte aligned (Hz % 4 == 0, kz0 a multiple of QW); chunks
@@ -1702,7 +1706,7 @@ static cudaError_t launch_kx_reg(const PassArgs<R>& a0, int runs, cudaStream_t s
   static cudaError_t attr_d = set_smem(kx_reg_kernel<R, N, MODE, true>, Sh::smem);
   if (attr_d != cudaSuccess) return attr_d;
   if constexpr (MODE == KX_STAGE) {
-    static cudaError_t attr_s = first_error({set_smem(kx_reg_kernel<R, N, MODE, true, 1>, Sh::smem),
+    static cudaError_t attr_s = first_error({set_smem(kx_reg_kernel<R, N, MODE, true, 1>, Sh::smem1),
                                              set_smem(kx_reg_kernel<R, N, MODE, true, 2>, Sh::smem),
                                              set_smem(kx_reg_kernel<R, N, MODE, true, 3>, Sh::smem),
                                              set_smem(kx_reg_kernel<R, N, MODE, true, 4>, Sh::smem)});
@@ -1716,7 +1720,7 @@ static cudaError_t launch_kx_reg(const PassArgs<R>& a0, int runs, cudaStream_t s
   if (MODE == KX_STAGE && Sh::PERSIST && resident > 0) ctas = std::min(a.tiles, resident);
   if (MODE == KX_STAGE && a.g.K == N / 3) {  // default cutoff: geometry and RK4 stage at compile time
     switch (a.stage) {
-      case 1: kx_reg_kernel<R, N, MODE, true, 1><<<ctas, Sh::NT, Sh::smem, st>>>(a); break;
+      case 1: kx_reg_kernel<R, N, MODE, true, 1><<<ctas, Sh::NT, Sh::smem1, st>>>(a); break;
       case 2: kx_reg_kernel<R, N, MODE, true, 2><<<ctas, Sh::NT, Sh::smem, st>>>(a); break;
       case 3: kx_reg_kernel<R, N, MODE, true, 3><<<ctas, Sh::NT, Sh::smem, st>>>(a); break;
       default: kx_reg_kernel<R, N, MODE, true, 4><<<ctas, Sh::NT, Sh::smem, st>>>(a); break;
