@@ -456,26 +456,36 @@ def run_ours(args, rank, world, local_rank):
         series_host = torch.empty((1 + K // SAVE_EVERY + (1 if K % SAVE_EVERY else 0), 1, 8),
                                   dtype=torch.float64).pin_memory()
         final_host = torch.empty_like(init_host).pin_memory()
-        barrier()
-        torch.cuda.synchronize(dev)
-        e2 = torch.cuda.Event(enable_timing=True)
-        e3 = torch.cuda.Event(enable_timing=True)
-        e2.record(stream)
-        state.copy_(init_host, non_blocking=True)
-        series = plan.run(state, dt=DT, nu=NU, nsteps=K, save_every=SAVE_EVERY)
-        series_host.copy_(series, non_blocking=True)
-        final_host.copy_(state, non_blocking=True)
-        e3.record(stream)
-        torch.cuda.synchronize(dev)
-        barrier()
+
+        def e2e_call():
+            barrier()
+            torch.cuda.synchronize(dev)
+            e2 = torch.cuda.Event(enable_timing=True)
+            e3 = torch.cuda.Event(enable_timing=True)
+            e2.record(stream)
+            state.copy_(init_host, non_blocking=True)
+            series = plan.run(state, dt=DT, nu=NU, nsteps=K, save_every=SAVE_EVERY)
+            series_host.copy_(series, non_blocking=True)
+            final_host.copy_(state, non_blocking=True)
+            e3.record(stream)
+            torch.cuda.synchronize(dev)
+            barrier()
+            return e2.elapsed_time(e3)
+
+        # one untimed call (first use of the run path's kernels and of the pinned buffers), then
+        # the median of three timed calls, each K steps from the host-resident initial state
+        e2e_call()
+        calls = sorted(e2e_call() for _ in range(3))
         e2e_launches = plan.last_launch_count
-        _, e2e_value = replica_throughput(e2.elapsed_time(e3), K, world, dev)
+        _, e2e_value = replica_throughput(calls[1], K, world, dev)
         sbytes = init_host.numel() * init_host.element_size()
         e2e = {"value": e2e_value, "unit": UNIT,
                "h2d_bytes_per_step": sbytes / K,
                "d2h_bytes_per_step": (sbytes + series_host.numel() * 8) / K,
                "path": "Plan.run (tg_run via ctypes): initial state H2D from pinned host memory, "
-                       f"{K} steps with diagnostics every {SAVE_EVERY}, series and final state D2H",
+                       f"{K} steps with diagnostics every {SAVE_EVERY}, series and final state D2H; "
+                       "median of 3 timed calls after 1 untimed call",
+               "calls_ms": calls,
                "gpu_launches": e2e_launches,
                "final_energy": float(series_host[-1, 0, 0])}
 
@@ -494,8 +504,8 @@ def run_ours(args, rank, world, local_rank):
     traffic = ncu_traffic(dom)
     roofline = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                 "traffic": traffic, "kernel": dom, "peak_source": f"{peak_kind} hbm_gbs",
-                "traffic_source": "profiles/dram_bytes_256.txt: committed ncu capture (not measured "
-                                  "in this run); the x stage's stage-3 launch",
+                "traffic_source": "profiles/dram_bytes_256.txt: this kernel's DRAM bytes from a committed "
+                                  "ncu capture (not measured in this run)",
                 "alg_bytes_per_launch": abytes[dom]}
     step_alg = step_bytes(n)
 
