@@ -152,7 +152,7 @@ def measure_ensemble(steps=50, count=64):
             "batched_runs_steps_per_s": count * steps / t_b, "speedup_vs_sequential": t_s / t_b,
             "batched_gpu_launches": launches, "per_size": per_size,
             "note": "batched = one plan per size (all runs of a size per launch, per-run nu/dt), "
-                    "groups on concurrent streams, step graphs; sequential = one plan per run, "
+                    "groups one after another on one stream, step graphs; sequential = one plan per run, "
                     "run after run"}
 
 

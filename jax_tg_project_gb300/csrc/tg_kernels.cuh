@@ -287,8 +287,8 @@ kx_kernel(const PassArgs<R> a) {
         return field_value<C>(map, gi, sb, ic, col, M, TZ, float(ksigned(ic, K)), kyf, kzf);
       };
       C* xg = xo + gi * g.sX;
-      auto dst = [&](int, int, int x, C v) {
-        if (zok) xg[(long long)x * M * Hz] = v;
+      auto dst = [&](int, int, int x, C v) {  // padding columns (kz >= Hk) get the zeros they hold
+        if (kz < Hz) xg[(long long)x * M * Hz] = v;
       };
       fft_column<Plan, +1>(t, src, dst, xcol, tw);
     }
@@ -333,8 +333,8 @@ ky_kernel(const PassArgs<R> a) {
   auto src = [&](int, int q) -> C { return pre[q]; };
   if constexpr (DIR > 0) {
     C* out = a.out + ((long long)run * a.nin + f) * g.sY + (long long)x * N * Hz + kz;
-    auto dst = [&](int, int, int y, C v) {
-      if (zok) out[(long long)y * Hz] = v;
+    auto dst = [&](int, int, int y, C v) {  // padding columns (kz >= Hk) get the zeros they hold
+      if (kz < Hz) out[(long long)y * Hz] = v;
     };
     fft_column<Plan, +1, 4, true, 0, true>(t, src, dst, xcol, tw);  // twiddle powers in registers
   } else {
@@ -342,7 +342,7 @@ ky_kernel(const PassArgs<R> a) {
     auto dst = [&](int b, int r, int k, C v) {
       if (slot_cut<N, P>(out_slot<Plan>(b, r))) return;  // always-removed rows
       const int ic = kcompact(k, N, K);
-      if (zok && ic >= 0) out[(long long)ic * Hz] = v;
+      if (kz < Hz && ic >= 0) out[(long long)ic * Hz] = v;  // zeros in the padding columns
     };
     fft_column<Plan, -1, 4, true, 0, true>(t, src, dst, xcol, tw);
   }
@@ -406,7 +406,12 @@ kz_kernel(const PassArgs<R> a) {
   };
   // unpack Z (in shared memory, natural order) into rows (x,y0) and (x,y0+1), kz <= K
   auto unpack_store = [&](const C* zb, C* outf) {
-    for (int k = t; k <= K; k += P) {
+    for (int k = t; k < Hz; k += P) {
+      if (k > K) {  // the rows' padding: whole 32-byte sectors written, no read-modify-write
+        outf[row0 + k] = czero<C>();
+        outf[row0 + Hz + k] = czero<C>();
+        continue;
+      }
       const C zk = zb[padx(k)];
       const C zm = zb[padx((N - k) % N)];
       const C A = mk<C>((zk.x + zm.x) * R(0.5), (zk.y - zm.y) * R(0.5));

@@ -225,6 +225,9 @@ __global__ void __launch_bounds__(128, KzRegShape<R, N>::MINB) kz_reg_kernel(con
       if (k <= K) {
         outf[k] = mk<C>((z[q].x + zm[q].x) * R(0.5), (z[q].y - zm[q].y) * R(0.5));
         outf[Hz + k] = mk<C>((z[q].y + zm[q].y) * R(0.5), (zm[q].x - z[q].x) * R(0.5));
+      } else if (k < Hz) {  // the rows' padding: whole 32-byte sectors written, no read-modify-write
+        outf[k] = czero<C>();
+        outf[Hz + k] = czero<C>();
       }
     }
   }
@@ -340,6 +343,9 @@ __global__ void __launch_bounds__(128, 3) kz_reg_mhd_kernel(const PassArgs<R> a)
       if (k <= K) {
         outf[k] = mk<C>((z[q].x + zm[q].x) * R(0.5), (z[q].y - zm[q].y) * R(0.5));
         outf[Hz + k] = mk<C>((z[q].y + zm[q].y) * R(0.5), (zm[q].x - z[q].x) * R(0.5));
+      } else if (k < Hz) {  // the rows' padding: whole 32-byte sectors written, no read-modify-write
+        outf[k] = czero<C>();
+        outf[Hz + k] = czero<C>();
       }
     }
   };
@@ -516,6 +522,9 @@ __global__ void __launch_bounds__(128, 3) kz_reg_adj_kernel(const PassArgs<R> a)
       if (k <= K) {
         outf[k] = mk<C>((z[q].x + zm[q].x) * R(0.5), (z[q].y - zm[q].y) * R(0.5));
         outf[Hz + k] = mk<C>((z[q].y + zm[q].y) * R(0.5), (zm[q].x - z[q].x) * R(0.5));
+      } else if (k < Hz) {  // the rows' padding: whole 32-byte sectors written, no read-modify-write
+        outf[k] = czero<C>();
+        outf[Hz + k] = czero<C>();
       }
     }
   };
@@ -851,6 +860,20 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
         } else {
 #pragma unroll
           for (int f = 0; f < 3; ++f) v[f][q] = czero<C>();
+          // padding columns: zeros, so that every 32-byte sector of a row is written whole
+          // (no read-modify-write of partly written sectors in the L2)
+          if (!zok && kz < Hz && ic >= 0) {
+#pragma unroll
+            for (int f = 0; f < 3; ++f) {
+              const long long o = soff + ((long long)f * M + ic) * M * Hz;
+              if (stage < 4) {
+                a.acc[o] = czero<C>();
+                if (expl) a.vs[o] = czero<C>();
+              } else {
+                a.S[o] = czero<C>();
+              }
+            }
+          }
         }
       }
       // the next tile: its state / accumulator tiles into the staging area (every thread of
@@ -888,8 +911,8 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
     auto inverse_of = [&](const C* in, int gi) {
       auto src = [&](int, int q) -> C { return in[q]; };
       C* xg = xo + gi * g.sX;
-      auto dst = [&](int, int, int x, C val) {
-        if (zok) xg[(long long)x * M * Hz] = val;
+      auto dst = [&](int, int, int x, C val) {  // padding columns (kz >= Hk) get the zeros they hold
+        if (kz < Hz) xg[(long long)x * M * Hz] = val;
       };
       run_fft(src, dst, Inv());
     };
@@ -1092,7 +1115,18 @@ __global__ void __launch_bounds__(KxStashShape<R, N>::NT, KxStashShape<R, N>::MI
           if (slot_cut<N, P>(q)) continue;
           const int qi = kept_slot_rank<N, P>(q);
           const int ic = kcompact_slot<N, P>(t, q, K);
-          if (!(zok && ic >= 0)) continue;  // stash entry already zero
+          if (!(zok && ic >= 0)) {  // stash entry already zero
+            if (!zok && kz < Hz && ic >= 0) {  // padding columns: zeros, whole sectors written
+              const long long o = soff + ((long long)f * M + ic) * M * Hz;
+              if (stage < 4) {
+                a.acc[o] = czero<C>();
+                if (expl) a.vs[o] = czero<C>();
+              } else {
+                a.S[o] = czero<C>();
+              }
+            }
+            continue;
+          }
           const long long o = soff + ((long long)f * M + ic) * M * Hz;
           const C n = st[(f * NK + qi) * GT];
           const C s = sv[qi];
@@ -1159,8 +1193,8 @@ __global__ void __launch_bounds__(KxStashShape<R, N>::NT, KxStashShape<R, N>::MI
     auto inverse_of = [&](const C* in, int gi) {
       auto src = [&](int, int q) -> C { return in[q]; };
       C* xg = xo + gi * g.sX;
-      auto dst = [&](int, int, int x, C val) {
-        if (zok) xg[(long long)x * M * Hz] = val;
+      auto dst = [&](int, int, int x, C val) {  // padding columns (kz >= Hk) get the zeros they hold
+        if (kz < Hz) xg[(long long)x * M * Hz] = val;
       };
       run_fft(src, dst, Inv());
     };

@@ -1,5 +1,5 @@
-"""Batched ensembles: every run of a batched, concurrent ensemble equals the same
-run done alone, and matches the NumPy oracle."""
+"""Batched ensembles: every run of a batched ensemble (groups in order on one stream, or on
+concurrent streams) equals the same run done alone, and matches the NumPy oracle."""
 import numpy as np
 import pytest
 
@@ -10,7 +10,8 @@ from oracle import tg_numpy as T
 pytestmark = pytest.mark.gpu
 
 
-def test_ensemble_runs_equal_single_runs(monkeypatch):
+@pytest.mark.parametrize("concurrent", [False, True])
+def test_ensemble_runs_equal_single_runs(monkeypatch, concurrent):
     """Bit-identical: each single run uses the pass variant its autotuned group chose."""
     import torch
 
@@ -18,7 +19,7 @@ def test_ensemble_runs_equal_single_runs(monkeypatch):
     from jax_tg_project_gb300.ensemble import Ensemble, RunSpec
     runs = [RunSpec(32, 400.0), RunSpec(24, 150.0), RunSpec(32, 2000.0), RunSpec(16, 900.0),
             RunSpec(24, 3000.0), RunSpec(32, 120.0)]
-    ens = Ensemble(runs, dt=2e-3, pert_amp=1e-2, k0=3.0, seed=5)
+    ens = Ensemble(runs, dt=2e-3, pert_amp=1e-2, k0=3.0, seed=5, concurrent=concurrent)
     ens.step(6)
     torch.cuda.synchronize()
     for i, r in enumerate(runs):
