@@ -725,6 +725,13 @@ static cudaError_t launch_ky_conf(const PassArgs<R>& a, int runs, cudaStream_t s
   if constexpr (sizeof(R) == 4) {  // FP32 plans: the default cutoff's geometry at compile time
     static cudaError_t attr_d = set_smem(ky_kernel<R, N, DIR, YC, true>, smem);
     if (attr_d != cudaSuccess) return attr_d;
+    // a shared-memory carveout of 58 % (132 KB): fewer y CTAs per SM than the default and a
+    // larger L1, which the columns' global loads need in flight (256^3 y 76.0 / 41.3 -> 74.7 /
+    // 39.3 us, MHD 128^3 step 0.404 -> 0.380 ms; 100 % or 6 CTAs a SM: y 98 / 56 us)
+    static cudaError_t attr_c = first_error(
+        {cudaFuncSetAttribute(ky_kernel<R, N, DIR, YC, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 58),
+         cudaFuncSetAttribute(ky_kernel<R, N, DIR, YC>, cudaFuncAttributePreferredSharedMemoryCarveout, 58)});
+    if (attr_c != cudaSuccess) return attr_c;
     if (a.g.K == N / 3) {
       ky_kernel<R, N, DIR, YC, true><<<grid, NT, smem, st>>>(a);
       return cudaGetLastError();
