@@ -686,8 +686,10 @@ __device__ __forceinline__ auto uw_field(const A& v, int q, float kx, float ky, 
 // in the order blockIdx.x, + gridDim.x, ...  With Sh::PERSIST (KX_STAGE), persistent CTAs
 // take the tiles in kz-fastest order: the twiddles are built once per CTA, and while a
 // tile's inverse transforms run, the state / accumulator tiles of the CTA's next tile are
-// staged into shared memory (cp.async) and its forward inputs are prefetched into L2, so that
-// a tile starts with its operands at hand.  Otherwise one tile per CTA, ky fastest.
+// staged into shared memory (cp.async), so that a tile starts with its operands at hand.  Its
+// forward inputs W are mostly still in L2 (the forward y pass writes them with an evict_last
+// policy); an explicit L2 prefetch of them, issued here before that, measured 1 % slower once
+// they were (118.1 -> 116.7 us without it).  Otherwise one tile per CTA, ky fastest.
 template <typename R, int N, int MODE, bool DEFK = false, int STG = 0>
 __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) kx_reg_kernel(const PassArgs<R> a) {
   using C = cplx<R>;
@@ -877,20 +879,12 @@ __global__ void __launch_bounds__(KxRegShape<R, N>::NT, KxRegShape<R, N>::MINB) 
         }
       }
       // the next tile: its state / accumulator tiles into the staging area (every thread of
-      // the group is past its reads of this tile's), its forward inputs into L2
+      // the group is past its reads of this tile's)
       const int next = tile + gridDim.x;
       if (next < a.tiles) {
         const int nbkz = tile_bkz(next), niyc = tile_iyc(next), nrun = next / (kzb * M);
         gsync();
         stage_state(niyc, nbkz, nrun);
-        const int nkz0 = (nbkz * Sh::NG + grp) * QW;
-        if (nkz0 < g.Hk) {
-          const C* nw = a.in + (long long)nrun * 3 * g.sX + (long long)niyc * Hz + nkz0;
-          for (int r = lt; r < 3 * N; r += GT) {  // one 32-byte row segment each
-            const C* ptr = nw + (long long)(r / N) * g.sX + (long long)(r % N) * M * Hz;
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
-          }
-        }
       }
     }
 
